@@ -1,0 +1,413 @@
+/*
+ * scir_oracle.c -- CPU oracle for the batched-filtering path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the
+ * smoke check and the CPU-baseline leg of bench.py call it to produce the
+ * expected outputs.  The shipped library never links or calls it, and no
+ * product code path falls back to it.
+ *
+ * Two kinds of functions live here:
+ *
+ *  1. Restatements of the reference's own CPU loops (SciR, a Rust workspace
+ *     that cannot be compiled in this environment).  Loop order, accumulation
+ *     type, operation order and tap orientation follow the cited lines so that
+ *     the f32 restatement reproduces the reference bit for bit:
+ *       - crates/scir-gpu/src/lib.rs:1134-1152  fir1d_batched_f32
+ *       - crates/scir-gpu/src/lib.rs:1166-1184  fir1d_batched_f64
+ *       - crates/scir-iir-filters/src/filter.rs:50-61   DirectForm2Transposed
+ *       - crates/scir-signal/src/lib.rs:260-267  sosfilt
+ *       - crates/scir-signal/src/lib.rs:278-291  filtfilt (no padding, zero state)
+ *       - crates/scir-signal/src/lib.rs:293-303  convolve (naive full convolution)
+ *       - crates/scir-signal/src/lib.rs:313-362  resample_poly (zero-stuff,
+ *         full convolution, decimate from offset (len(h)-1)/2); the reference
+ *         hard-wires up=2/down=3 and a 31-tap table, the restatement takes the
+ *         rates and taps as arguments.
+ *
+ *  2. FP64 restatements of the SciPy semantics that the generalised entry
+ *     points follow (numpy.convolve modes, scipy.signal.upfirdn,
+ *     resample_poly, sosfilt_zi / lfilter_zi, sosfiltfilt with odd padding).
+ *     They restate SciPy's published algorithms and are pinned against
+ *     SciPy itself in the CPU test suite.
+ *
+ * Compile with -ffp-contract=off: the reference (Rust) never fuses a multiply
+ * and an add, and the f32 restatement must not either.
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_API __attribute__((visibility("default")))
+
+ORC_API int orc_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* FIR, reference orientation                                               */
+/* ------------------------------------------------------------------------ */
+
+/* crates/scir-gpu/src/lib.rs:1134-1152.  For each row and each output i, the
+ * reference walks the input backwards from xi=i down to start=max(i+1-k,0),
+ * pairing the t-th visited sample with taps[k-1-t], and accumulates in f32
+ * with a separate multiply and add: y[i] = sum_t taps[k-1-t]*x[i-t]. */
+ORC_API void orc_fir1d_batched_f32(const float* x, int64_t b, int64_t n,
+                                   const float* taps, int64_t k, float* y) {
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t bi = 0; bi < b; ++bi) {
+        const float* xr = x + bi * n;
+        float* yr = y + bi * n;
+        for (int64_t i = 0; i < n; ++i) {
+            float acc = 0.0f;
+            int64_t start = (i + 1 > k) ? (i + 1 - k) : 0;
+            int64_t t = 0;
+            for (int64_t xi = i; xi >= start; --xi, ++t) {
+                float prod = taps[k - 1 - t] * xr[xi];
+                acc = acc + prod;
+            }
+            yr[i] = acc;
+        }
+    }
+}
+
+/* crates/scir-gpu/src/lib.rs:1166-1184: the same loop in f64. */
+ORC_API void orc_fir1d_batched_f64(const double* x, int64_t b, int64_t n,
+                                   const double* taps, int64_t k, double* y) {
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t bi = 0; bi < b; ++bi) {
+        const double* xr = x + bi * n;
+        double* yr = y + bi * n;
+        for (int64_t i = 0; i < n; ++i) {
+            double acc = 0.0;
+            int64_t start = (i + 1 > k) ? (i + 1 - k) : 0;
+            int64_t t = 0;
+            for (int64_t xi = i; xi >= start; --xi, ++t) {
+                double prod = taps[k - 1 - t] * xr[xi];
+                acc = acc + prod;
+            }
+            yr[i] = acc;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* FIR, generalised modes (FP64 truth)                                      */
+/* ------------------------------------------------------------------------ */
+
+/* Mode numbering shared with the library's C ABI:
+ *   0  reference correlation, len n:  y[i] = sum_m taps[m] x[i-(k-1)+m]
+ *   1  lfilter(taps, 1, x), len n:     y[i] = sum_j taps[j] x[i-j]
+ *   2  numpy.convolve(x, taps,'full'), len n+k-1
+ *   3  numpy.convolve(x, taps,'valid'), len n-k+1 (n >= k)
+ * Every mode is written as a correlation c[m] against x[o + s + m] with
+ * x zero outside [0, n); modes 1-3 use the reversed taps. */
+ORC_API int64_t orc_fir_out_len(int64_t n, int64_t k, int mode) {
+    switch (mode) {
+    case 0: case 1: return n;
+    case 2: return n + k - 1;
+    case 3: return n >= k ? n - k + 1 : -1;
+    default: return -1;
+    }
+}
+
+ORC_API int orc_fir_mode_f64(const double* x, int64_t b, int64_t n,
+                             const double* taps, int64_t k, int mode,
+                             double* y) {
+    int64_t n_out = orc_fir_out_len(n, k, mode);
+    if (n_out < 0 || k < 1) return -1;
+    int64_t s = (mode == 3) ? 0 : -(k - 1);
+    double* c = (double*)malloc(sizeof(double) * (size_t)k);
+    if (!c) return -2;
+    for (int64_t m = 0; m < k; ++m) c[m] = (mode == 0) ? taps[m] : taps[k - 1 - m];
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t bi = 0; bi < b; ++bi) {
+        const double* xr = x + bi * n;
+        double* yr = y + bi * n_out;
+        for (int64_t o = 0; o < n_out; ++o) {
+            int64_t lo = o + s;
+            int64_t m0 = lo < 0 ? -lo : 0;
+            int64_t m1 = (n - lo < k) ? (n - lo) : k;
+            double acc = 0.0;
+            for (int64_t m = m0; m < m1; ++m) acc += c[m] * xr[lo + m];
+            yr[o] = acc;
+        }
+    }
+    free(c);
+    return 0;
+}
+
+/* Ragged set: signal i has n[i] samples at x + x_off[i], its own taps at
+ * taps + t_off[i] (k[i] of them) and its output at y + y_off[i]; every signal
+ * uses the same mode. */
+ORC_API int orc_fir_ragged_f64(const double* x, const int64_t* x_off,
+                               const int64_t* n, const double* taps,
+                               const int64_t* t_off, const int64_t* k,
+                               int64_t count, int mode, double* y,
+                               const int64_t* y_off) {
+    int bad = 0;
+    #pragma omp parallel for schedule(dynamic, 1) reduction(|:bad)
+    for (int64_t i = 0; i < count; ++i) {
+        if (orc_fir_mode_f64(x + x_off[i], 1, n[i], taps + t_off[i], k[i], mode,
+                             y + y_off[i]) != 0)
+            bad |= 1;
+    }
+    return bad ? -1 : 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Second-order sections                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* crates/scir-iir-filters/src/filter.rs:50-61 (DirectForm2Transposed::filter)
+ * driven per sample as in crates/scir-signal/src/lib.rs:260-267.  The SOS
+ * matrix is [nsec][6] = b0 b1 b2 a0 a1 a2 (crates/scir-iir-filters/src/sos.rs:
+ * 49-66); a0 is assumed to be 1 and never read, as in the reference.
+ * zi/zf, when non-NULL, are [b][nsec][2] (s1, s2) initial/final states; the
+ * reference always starts from zero (zi == NULL). */
+ORC_API void orc_sosfilt_f64(const double* sos, int nsec, const double* x,
+                             int64_t b, int64_t n, const double* zi,
+                             double* zf, double* y) {
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t bi = 0; bi < b; ++bi) {
+        double s1[64], s2[64];
+        for (int s = 0; s < nsec; ++s) {
+            s1[s] = zi ? zi[(bi * nsec + s) * 2 + 0] : 0.0;
+            s2[s] = zi ? zi[(bi * nsec + s) * 2 + 1] : 0.0;
+        }
+        const double* xr = x + bi * n;
+        double* yr = y + bi * n;
+        for (int64_t i = 0; i < n; ++i) {
+            double out = xr[i];
+            for (int s = 0; s < nsec; ++s) {
+                const double* c = sos + 6 * s;
+                double prev = out;
+                out = c[0] * prev + s1[s];
+                s1[s] = c[1] * prev - c[4] * out + s2[s];
+                s2[s] = c[2] * prev - c[5] * out;
+            }
+            yr[i] = out;
+        }
+        if (zf) {
+            for (int s = 0; s < nsec; ++s) {
+                zf[(bi * nsec + s) * 2 + 0] = s1[s];
+                zf[(bi * nsec + s) * 2 + 1] = s2[s];
+            }
+        }
+    }
+}
+
+/* crates/scir-signal/src/lib.rs:278-291: forward DF2T pass, then a fresh
+ * zero-state pass over the reversed intermediate, reversed back.  No edge
+ * padding, no initial conditions. */
+ORC_API void orc_filtfilt_ref_f64(const double* sos, int nsec, const double* x,
+                                  int64_t b, int64_t n, double* y) {
+    double* tmp = (double*)malloc(sizeof(double) * (size_t)(b * n));
+    orc_sosfilt_f64(sos, nsec, x, b, n, NULL, NULL, tmp);
+    for (int64_t bi = 0; bi < b; ++bi) {
+        double* r = tmp + bi * n;
+        for (int64_t i = 0, j = n - 1; i < j; ++i, --j) { double t = r[i]; r[i] = r[j]; r[j] = t; }
+    }
+    orc_sosfilt_f64(sos, nsec, tmp, b, n, NULL, NULL, y);
+    for (int64_t bi = 0; bi < b; ++bi) {
+        double* r = y + bi * n;
+        for (int64_t i = 0, j = n - 1; i < j; ++i, --j) { double t = r[i]; r[i] = r[j]; r[j] = t; }
+    }
+    free(tmp);
+}
+
+/* SciPy sosfilt_zi: steady-state DF2T state of each section for a unit step,
+ * scaled by the DC gain of the sections before it.  Per section the state is
+ * SciPy's lfilter_zi closed form (a normalised so a0 = 1,
+ * y_inf = sum(b)/sum(a), d = b - y_inf*a, zi = reverse cumulative sum of d
+ * without its first element): zi0 = d1 + d2, zi1 = d2.
+ * Returns -1 when a section has sum(a) == 0 (pole at z = 1). */
+ORC_API int orc_sosfilt_zi(const double* sos, int nsec, double* zi) {
+    double scale = 1.0;
+    for (int s = 0; s < nsec; ++s) {
+        const double* c = sos + 6 * s;
+        double a0 = c[3];
+        if (a0 == 0.0) return -1;
+        double b0 = c[0], b1 = c[1], b2 = c[2], a1 = c[4], a2 = c[5];
+        if (a0 != 1.0) { b0 /= a0; b1 /= a0; b2 /= a0; a1 /= a0; a2 /= a0; a0 = 1.0; }
+        double suma = a0 + a1 + a2;
+        if (suma == 0.0) return -1;
+        double yinf = (b0 + b1 + b2) / suma;
+        double d1 = b1 - yinf * a1, d2 = b2 - yinf * a2;
+        zi[2 * s + 0] = scale * (d1 + d2);
+        zi[2 * s + 1] = scale * d2;
+        scale *= (c[0] + c[1] + c[2]) / (c[3] + c[4] + c[5]);
+    }
+    return 0;
+}
+
+/* SciPy's default filtfilt edge for an SOS cascade:
+ * 3 * (2*nsec + 1 - min(#(b2 == 0), #(a2 == 0))). */
+ORC_API int64_t orc_sosfiltfilt_default_padlen(const double* sos, int nsec) {
+    int zb = 0, za = 0;
+    for (int s = 0; s < nsec; ++s) {
+        if (sos[6 * s + 2] == 0.0) ++zb;
+        if (sos[6 * s + 5] == 0.0) ++za;
+    }
+    int z = zb < za ? zb : za;
+    return 3 * (int64_t)(2 * nsec + 1 - z);
+}
+
+/* SciPy sosfiltfilt with padtype 'odd' (padtype 0) or no padding (padtype -1):
+ * odd extension ext = [2x0 - x[edge..1], x, 2x[n-1] - x[n-2..n-1-edge]],
+ * forward pass from zi*ext[0], backward pass from zi*y[last], trim edges.
+ * padlen < 0 selects the default edge.  Returns -1 when n <= edge. */
+ORC_API int orc_sosfiltfilt_f64(const double* sos, int nsec, const double* x,
+                                int64_t b, int64_t n, int padtype,
+                                int64_t padlen, double* y) {
+    int64_t edge = padtype < 0 ? 0 : (padlen < 0 ? orc_sosfiltfilt_default_padlen(sos, nsec) : padlen);
+    if (n <= edge) return -1;
+    double zi[128];
+    if (nsec > 64 || orc_sosfilt_zi(sos, nsec, zi) != 0) return -2;
+    int64_t m = n + 2 * edge;
+    int bad = 0;
+    #pragma omp parallel for schedule(dynamic, 1) reduction(|:bad)
+    for (int64_t bi = 0; bi < b; ++bi) {
+        const double* xr = x + bi * n;
+        double* ext = (double*)malloc(sizeof(double) * (size_t)m * 2);
+        if (!ext) { bad |= 1; continue; }
+        double* tmp = ext + m;
+        for (int64_t i = 0; i < edge; ++i) ext[i] = 2.0 * xr[0] - xr[edge - i];
+        for (int64_t i = 0; i < n; ++i) ext[edge + i] = xr[i];
+        for (int64_t i = 0; i < edge; ++i) ext[edge + n + i] = 2.0 * xr[n - 1] - xr[n - 2 - i];
+        double z[128];
+        for (int s = 0; s < 2 * nsec; ++s) z[s] = zi[s] * ext[0];
+        orc_sosfilt_f64(sos, nsec, ext, 1, m, z, NULL, tmp);
+        /* reverse into ext, second pass from zi * last forward output */
+        double ylast = tmp[m - 1];
+        for (int64_t i = 0; i < m; ++i) ext[i] = tmp[m - 1 - i];
+        for (int s = 0; s < 2 * nsec; ++s) z[s] = zi[s] * ylast;
+        orc_sosfilt_f64(sos, nsec, ext, 1, m, z, NULL, tmp);
+        double* yr = y + bi * n;
+        for (int64_t i = 0; i < n; ++i) yr[i] = tmp[m - 1 - (edge + i)];
+        free(ext);
+    }
+    return bad ? -3 : 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Polyphase resampling                                                     */
+/* ------------------------------------------------------------------------ */
+
+static int64_t gcd64(int64_t a, int64_t b) { while (b) { int64_t t = a % b; a = b; b = t; } return a; }
+
+/* scipy.signal.upfirdn output length: ceil(((n - 1) * up + kh) / down). */
+ORC_API int64_t orc_upfirdn_out_len(int64_t kh, int64_t n, int64_t up, int64_t down) {
+    return (((n - 1) * up + kh) - 1) / down + 1;
+}
+
+/* scipy.signal.upfirdn: y[m] = sum_j h[j] * u[m*down - j], u the input
+ * zero-stuffed by `up` (u[t] = x[t/up] when up divides t). */
+ORC_API void orc_upfirdn_f64(const double* h, int64_t kh, const double* x,
+                             int64_t b, int64_t n, int64_t up, int64_t down,
+                             double* y, int64_t nout) {
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t bi = 0; bi < b; ++bi) {
+        const double* xr = x + bi * n;
+        double* yr = y + bi * nout;
+        for (int64_t mo = 0; mo < nout; ++mo) {
+            int64_t t = mo * down;
+            int64_t ph = t % up, base = t / up;
+            double acc = 0.0;
+            for (int64_t j = ph, q = 0; j < kh; j += up, ++q) {
+                int64_t xi = base - q;
+                if (xi < 0) break;
+                if (xi < n) acc += h[j] * xr[xi];
+            }
+            yr[mo] = acc;
+        }
+    }
+}
+
+/* resample_poly output length after reducing up/down by their gcd:
+ * ceil(n * up / down). */
+ORC_API int64_t orc_resample_poly_out_len(int64_t n, int64_t up, int64_t down) {
+    int64_t g = gcd64(up, down);
+    up /= g; down /= g;
+    return (n * up) / down + ((n * up) % down ? 1 : 0);
+}
+
+/* crates/scir-signal/src/lib.rs:313-362 with the rates and taps as arguments.
+ * Zero-stuff x by `up`, full convolution with h (crates/scir-signal/src/lib.rs:
+ * 293-303: every zero-stuffed sample, zero or not, is multiplied through all
+ * of h), then keep conv[off + m*down] for off = (kh-1)/2 while the index is
+ * below len(conv) - off.  The reference asserts up=2, down=3 and bakes its
+ * taps; for those arguments this is the same computation.  Rates are used as
+ * given (the reference does not reduce them). */
+ORC_API int64_t orc_resample_poly_ref_f64(const double* x, int64_t b, int64_t n,
+                                          int64_t up, int64_t down,
+                                          const double* h, int64_t kh,
+                                          double* y) {
+    int64_t nu = n * up;
+    int64_t nc = nu + kh - 1;
+    int64_t off = (kh - 1) / 2;
+    int64_t end = nc - off;
+    int64_t nout = 0;
+    for (int64_t idx = off; idx < end; idx += down) ++nout;
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t bi = 0; bi < b; ++bi) {
+        double* u = (double*)calloc((size_t)nu, sizeof(double));
+        double* conv = (double*)calloc((size_t)nc, sizeof(double));
+        const double* xr = x + bi * n;
+        for (int64_t i = 0; i < n; ++i) u[i * up] = xr[i];
+        for (int64_t i = 0; i < nu; ++i)
+            for (int64_t j = 0; j < kh; ++j)
+                conv[i + j] += u[i] * h[j];
+        double* yr = y + bi * nout;
+        int64_t m = 0;
+        for (int64_t idx = off; idx < end; idx += down) yr[m++] = conv[idx];
+        free(u);
+        free(conv);
+    }
+    return nout;
+}
+
+/* scipy.signal.resample_poly (zero-padded edges) in polyphase form, only the
+ * non-zero products: reduce up/down by their gcd (both 1: a copy), then
+ * y[m] = sum_q h[ph + q*up] x[base - q] for t = (kh-1)/2 + m*down,
+ * ph = t mod up, base = t div up, m < ceil(n*up/down).  For odd kh this is
+ * exactly the output of orc_resample_poly_ref_f64; it is the fast FP64 truth
+ * at sizes where the reference loop is too slow. */
+ORC_API int64_t orc_resample_poly_fast_f64(const double* x, int64_t b, int64_t n,
+                                           int64_t up, int64_t down,
+                                           const double* h, int64_t kh,
+                                           double* y) {
+    int64_t g = gcd64(up, down);
+    up /= g; down /= g;
+    int64_t nout = (n * up) / down + ((n * up) % down ? 1 : 0);
+    if (up == 1 && down == 1) {
+        memcpy(y, x, sizeof(double) * (size_t)(b * n));
+        return n;
+    }
+    int64_t off = (kh - 1) / 2;
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t bi = 0; bi < b; ++bi) {
+        const double* xr = x + bi * n;
+        double* yr = y + bi * nout;
+        for (int64_t mo = 0; mo < nout; ++mo) {
+            int64_t t = off + mo * down;
+            int64_t ph = t % up, base = t / up;
+            double acc = 0.0;
+            for (int64_t j = ph, q = 0; j < kh; j += up, ++q) {
+                int64_t xi = base - q;
+                if (xi < 0) break;
+                if (xi < n) acc += h[j] * xr[xi];
+            }
+            yr[mo] = acc;
+        }
+    }
+    return nout;
+}
