@@ -1,0 +1,435 @@
+#!/usr/bin/env python3
+"""Throughput of the batched-filtering hot path on GB300.
+
+Default workload (N=1): polyphase resample_poly 160/147 of 256 channels x
+1,048,576 f32 N(0,1) samples with SciPy's default 3,201-tap Kaiser(5.0)
+design -- the configuration the headline metric (batched FIR Gsamples/s,
+chosen vs plain FP32) is quoted on.  Other configurations can be timed with
+--workload (fir_short, fir_long, ragged, sosfilt, sosfiltfilt).
+
+A step is one pass of the hot path over one batch of synthetic input,
+resident in HBM.  W warm-up steps, then K timed steps between a barrier and
+a device synchronize; the device time comes from CUDA events on the launch
+stream, the max over ranks is reported by rank 0 as one JSON line.  Inputs
+are larger than L2 (129 MB) for the default workload.  `e2e` re-times the
+same work through the host-buffer C-ABI entry point (pinned host buffers,
+host<->device copies inside the timed region).  `cpu_baseline` times the CPU
+restatement of the reference's own algorithm on a bounded sample.
+
+--impl reference times the reference's CPU implementation of the path (the
+restated loops; the Rust reference cannot be compiled here) on the host cores
+with all threads.
+
+Multi-GPU: torchrun, one rank per GPU; every rank processes its own full batch
+of channels (weak scaling, no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+# FP32 FFMA throughput measured on this machine's GB300 with an independent-chain
+# FFMA loop (72.6 TFLOP/s); used only for CUDA-core-bound workloads.
+FP32_PEAK_TFLOPS = 72.6
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"]),
+                "bf16_tflops_sustained": float(d.get("bf16_tflops_sustained", d["bf16_tflops"])),
+                "source": "measured"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+                "source": "fallback"}
+
+
+def profile_traffic(workload: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (a line `traffic_bytes_per_launch: <n>` in profiles/<workload>*.md)."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for fn in sorted(os.listdir(pdir)):
+        if fn.startswith(workload) and fn.endswith(".md"):
+            with open(os.path.join(pdir, fn)) as f:
+                for line in f:
+                    if line.strip().startswith("traffic_bytes_per_launch:"):
+                        try:
+                            return float(line.split(":", 1)[1].split()[0])
+                        except ValueError:
+                            return None
+    return None
+
+
+# ----------------------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.tmp = None
+
+    def __enter__(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.tmp is None:
+            return None
+        self.tmp.flush()
+        self.tmp.seek(0)
+        rows = [r.split(",") for r in self.tmp.read().strip().splitlines() if r.strip()]
+        os.unlink(self.tmp.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [c.strip() for c in r]
+            if len(r) < 7:
+                continue
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, r[3:7]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ----------------------------------------------------------------------------- workloads
+
+class Workload:
+    name = ""
+    metric = "batched FIR Gsamples/s"
+    unit = "Gsamples/s"
+    bound = "hbm"
+    launches_per_step = 1
+
+    def samples_per_step(self) -> int:
+        raise NotImplementedError
+
+
+class Resample(Workload):
+    name = "resample_poly_160_147"
+    B, N, UP, DOWN = 256, 1048576, 160, 147
+
+    def __init__(self, torch, dev, precision):
+        import scir_gb300 as S
+        self.S, self.torch, self.dev = S, torch, dev
+        self.precision = precision
+        g = torch.Generator(device=dev).manual_seed(0)
+        self.x = torch.randn((self.B, self.N), device=dev, generator=g)
+        self.n_out = S.resample_poly_out_len(self.N, self.UP, self.DOWN)
+        self.y = torch.empty((self.B, self.n_out), device=dev)
+        self.kh = S.resample_poly_default_taps(self.UP, self.DOWN).size
+        self.kernel = "poly_fast_kernel"
+
+    @classmethod
+    def config(cls):
+        return {"workload": "resample_poly 160/147: 256 ch x 1,048,576 f32 N(0,1) samples, "
+                            "SciPy default 3,201-tap Kaiser(5.0) design, zero-padded edges",
+                "channels": cls.B, "samples_per_channel": cls.N, "up": cls.UP,
+                "down": cls.DOWN, "taps": 3201, "outputs_per_channel": 1141308,
+                "l2": "inputs larger than L2 (1.07 GB read, 1.17 GB written per step)"}
+
+    def samples_per_step(self):
+        return self.B * self.N
+
+    def alg_bytes(self):
+        return 4 * self.B * (self.N + self.n_out)
+
+    def alg_flops(self):
+        return 2.0 * self.B * self.n_out * (self.kh / self.UP)
+
+    def step(self, stream, precision=None):
+        self.S.resample_poly_f32(self.x, self.UP, self.DOWN, precision=self.precision if precision is None else precision,
+                                 out=self.y, stream=stream)
+
+    def max_rel_err(self, precision=None):
+        import scipy.signal as ss
+        rows = [0, self.B - 1]
+        self.step(None, precision)
+        self.torch.cuda.synchronize()
+        y = self.y[rows].cpu().numpy().astype(np.float64)
+        ref = ss.resample_poly(self.x[rows].cpu().numpy().astype(np.float64), self.UP, self.DOWN,
+                               axis=1)
+        return float(np.max(np.abs(y - ref)) / np.max(np.abs(ref)))
+
+    def host_setup(self):
+        t = self.torch
+        self.hx = t.empty((self.B, self.N), dtype=t.float32, pin_memory=True)
+        self.hx.copy_(self.x)
+        self.hy = t.empty((self.B, self.n_out), dtype=t.float32, pin_memory=True)
+        self.hx_np, self.hy_np = self.hx.numpy(), self.hy.numpy()
+        return 4 * self.B * self.N, 4 * self.B * self.n_out
+
+    def host_step(self):
+        self.S.resample_poly_host(self.hx_np, self.UP, self.DOWN, precision=self.precision,
+                                  out=self.hy_np)
+
+    # the reference's CPU algorithm (zero-stuff, full convolution, decimate)
+    def cpu_sample(self, O, threads, per_channel):
+        rng = np.random.default_rng(1)
+        x = rng.standard_normal((threads, per_channel))
+        h = self.S.resample_poly_default_taps(self.UP, self.DOWN)
+        t0 = time.perf_counter()
+        O.resample_poly_ref_f64(x, self.UP, self.DOWN, h)
+        return threads * per_channel, time.perf_counter() - t0
+
+    def cpu_sample_desc(self, threads, per_channel):
+        return (f"{threads} channels x {per_channel} samples per step through the restated "
+                f"reference resample_poly (zero-stuff by 160, full 3,201-tap convolution, "
+                f"decimate by 147), f64, one OpenMP thread per channel")
+
+
+WORKLOADS = {"resample": Resample}
+
+
+# ----------------------------------------------------------------------------- runners
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def smi_index(local_rank: int) -> int:
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        parts = [p.strip() for p in vis.split(",") if p.strip()]
+        if local_rank < len(parts) and parts[local_rank].isdigit():
+            return int(parts[local_rank])
+    return local_rank
+
+
+def calibrate_cpu(W, O, threads, target_s):
+    per = 64
+    while True:
+        n, dt = W.cpu_sample(O, threads, per)
+        if dt >= 0.25 or per >= 1 << 22:
+            break
+        per *= 4
+    per = max(16, int(per * target_s / max(dt, 1e-6)))
+    return per
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle as O
+    import torch  # noqa: F401  (same interpreter as the GPU arm)
+
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    W = WORKLOADS[args.workload].__new__(WORKLOADS[args.workload])
+    import scir_gb300 as S
+    W.S = S
+    per_step_s = max(0.5, min(3.0, 90.0 / max(1, args.steps + args.warmup)))
+    per = calibrate_cpu(W, O, threads, per_step_s)
+    for _ in range(args.warmup):
+        W.cpu_sample(O, threads, per)
+    total_n, total_t = 0, 0.0
+    for _ in range(args.steps):
+        n, dt = W.cpu_sample(O, threads, per)
+        total_n += n
+        total_t += dt
+    value = total_n / total_t / 1e9
+    cfg = WORKLOADS[args.workload].config()
+    line = {"impl": "reference", "metric": W.metric, "value": value, "unit": W.unit,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000 * total_t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": cfg,
+            "cpu_baseline": {"value": value, "unit": W.unit, "cores": threads, "kind": "port",
+                             "sample": W.cpu_sample_desc(threads, per)},
+            "e2e": {"value": value, "unit": W.unit, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference is Rust and no Rust toolchain exists here or on the GPU box; "
+                    "this arm times the C restatement of its CPU loop"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import scir_gb300 as S
+
+    rank, world, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+    peaks = load_peaks()
+    prec = S.Precision[args.precision]
+    W = WORKLOADS[args.workload](torch, dev, prec)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier(device_ids=[local])
+
+    for _ in range(max(3, args.warmup)):
+        W.step(stream)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(smi_index(local)) as clk:
+        time.sleep(0.3)  # let the sampler start before the timed region
+        evs[0].record(stream)
+        for i in range(args.steps):
+            W.step(stream)
+            evs[i + 1].record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    per_step = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
+    total_ms = evs[0].elapsed_time(evs[-1])
+    t = torch.tensor([total_ms], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = world * W.samples_per_step() * args.steps / (total_ms / 1e3) / 1e9
+
+    # plain FP32 on the same inputs, for the chosen-vs-plain comparison
+    plain = None
+    if prec != S.Precision.FP32:
+        for _ in range(3):
+            W.step(stream, S.Precision.FP32)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            W.step(stream, S.Precision.FP32)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pms = e0.elapsed_time(e1) / args.steps
+        plain = {"value": W.samples_per_step() / (pms / 1e3) / 1e9, "unit": W.unit,
+                 "ms_per_step": pms}
+    err = W.max_rel_err()
+
+    # end to end through the host-buffer C-ABI call
+    h2d, d2h = W.host_setup()
+    W.host_step()
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        W.host_step()
+    torch.cuda.synchronize()
+    e2e_s = torch.tensor([time.perf_counter() - t0], device=dev, dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(e2e_s, op=dist.ReduceOp.MAX)
+    e2e_value = world * W.samples_per_step() * args.steps / float(e2e_s.item()) / 1e9
+
+    # roofline of the dominant kernel (one launch per step)
+    kern_ms = statistics.mean(per_step) / W.launches_per_step
+    if W.bound == "hbm":
+        achieved = W.alg_bytes() / (kern_ms / 1e3) / 1e9
+        peak, unit = peaks["hbm_gbs"], "GB/s"
+    else:
+        achieved = W.alg_flops() / (kern_ms / 1e3) / 1e12
+        peak, unit = FP32_PEAK_TFLOPS, "TFLOP/s"
+    traffic = profile_traffic(W.name)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        import oracle as O
+        threads = os.cpu_count() or 1
+        O.set_threads(threads)
+        per = calibrate_cpu(W, O, threads, 3.0)
+        tot_n, tot_t = 0, 0.0
+        for _ in range(3):
+            n, dt = W.cpu_sample(O, threads, per)
+            tot_n += n
+            tot_t += dt
+        cpu = {"value": tot_n / tot_t / 1e9, "unit": W.unit, "cores": threads, "kind": "port",
+               "sample": W.cpu_sample_desc(threads, per)}
+    clocks = clk.summary()
+    if world > 1:
+        dist.destroy_process_group()
+    if rank != 0:
+        return 0
+    line = {
+        "metric": W.metric, "value": value, "unit": W.unit, "n_gpus": world,
+        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded torch.randn on the device)",
+        "config": dict(W.config(), precision=prec.name, parallelism=f"replicas x{world}"),
+        "roofline": {"bound": W.bound, "achieved": achieved, "peak": peak, "unit": unit,
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": W.kernel, "kernel_ms": kern_ms,
+                     "peak_source": peaks["source"] if W.bound == "hbm" else "probe"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": W.unit, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": W.launches_per_step * args.steps,
+        "max_rel_err_vs_fp64": err,
+        "plain_fp32": plain,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="resample")
+    ap.add_argument("--precision", default="AUTO")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,302 @@
+/*
+ * scir_gb300.h -- C ABI of the GB300 (sm_103a) batched-filtering library.
+ *
+ * This is the boundary a SciR build binds over FFI in place of the CUDA
+ * module inside crates/scir-gpu.  Two layers are exported:
+ *
+ *  - Stream-ordered device entry points (scir_fir_batched_f32, ...): every
+ *    pointer is a device pointer, every call is asynchronous on the caller's
+ *    cudaStream_t (NULL = legacy default stream) and returns a status code.
+ *    Buffers are caller-owned, rows are strided by ld_* elements.
+ *
+ *  - Host-buffer entry points named after the reference's Rust functions
+ *    (scir_fir1d_batched_f32_cuda, scir_sosfilt_f64, ...): plain host
+ *    pointers in, host pointers out, synchronous, exactly the semantics of
+ *    the function they replace.  These are what the Rust FFI crate calls to
+ *    keep the scir-gpu / scir-signal signatures.
+ *
+ * Every function returns SCIR_OK (0) or an scir_status error code; the
+ * thread-local detail is available from scir_last_error().  No function falls
+ * back to a CPU implementation: when the CUDA device or the compiled kernels
+ * are unavailable the call fails with SCIR_ERR_NO_DEVICE / SCIR_ERR_CUDA.
+ *
+ * Threading: calls may come from any host thread; the library keeps only
+ * per-device immutable data and a mutex-protected staging pool for the
+ * host-buffer layer.  Device entry points never synchronise the stream.
+ */
+#ifndef SCIR_GB300_H
+#define SCIR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SCIR_API __attribute__((visibility("default")))
+#else
+#define SCIR_API
+#endif
+
+#define SCIR_GB300_ABI_VERSION 1
+
+/* Status codes.  The reference reports GPU failures as
+ * GpuError::{BackendUnavailable(String), ShapeMismatch}
+ * (crates/scir-gpu/src/lib.rs:58-63); the FFI crate maps SCIR_ERR_SHAPE to
+ * ShapeMismatch and every other code to BackendUnavailable(message). */
+typedef enum scir_status {
+    SCIR_OK = 0,
+    SCIR_ERR_INVALID_ARG = 1, /* null pointer, negative size, bad enum      */
+    SCIR_ERR_SHAPE = 2,       /* sizes inconsistent (n < k for VALID, ...)  */
+    SCIR_ERR_ALIGN = 3,       /* pointer/stride alignment a kernel requires */
+    SCIR_ERR_OOM = 4,         /* device or pinned allocation failed         */
+    SCIR_ERR_CUDA = 5,        /* CUDA runtime error (message has details)   */
+    SCIR_ERR_TIMEOUT = 6,     /* bounded device-side wait gave up           */
+    SCIR_ERR_UNSUPPORTED = 7, /* valid request this build does not serve    */
+    SCIR_ERR_NO_DEVICE = 8    /* no CUDA device / kernel image for it       */
+} scir_status;
+
+/* FIR output conventions.  Every mode is computed as
+ *   y[o] = sum_{m<k} c[m] * x[o + s + m],  x = 0 outside [0, n)
+ * SCIR_FIR_REF_CORR: the reference fir1d_batched_f32 (crates/scir-gpu/src/
+ *   lib.rs:1134-1152): c = taps, s = -(k-1), n outputs, i.e.
+ *   y[i] = sum_j taps[k-1-j] * x[i-j]  (= scipy lfilter(taps[::-1], 1, x)).
+ * SCIR_FIR_LFILTER: scipy.signal.lfilter(taps, 1, x): c = reversed taps,
+ *   s = -(k-1), n outputs.
+ * SCIR_FIR_FULL / SCIR_FIR_VALID: numpy.convolve(x, taps, 'full'|'valid'):
+ *   n+k-1 outputs / n-k+1 outputs (VALID needs n >= k). */
+typedef enum scir_fir_mode {
+    SCIR_FIR_REF_CORR = 0,
+    SCIR_FIR_LFILTER = 1,
+    SCIR_FIR_FULL = 2,
+    SCIR_FIR_VALID = 3
+} scir_fir_mode;
+
+/* Arithmetic used for a FIR / polyphase contraction.
+ * SCIR_PREC_REF_EXACT: FP32 on CUDA cores with the reference's summation
+ *   order and separate multiply/add roundings (no FMA): bit-identical to
+ *   the reference CPU loop for SCIR_FIR_REF_CORR.
+ * SCIR_PREC_FP32: FP32 FMA on CUDA cores ("plain").
+ * SCIR_PREC_BF16X3: tensor cores (tcgen05, kind::f16), operands split into
+ *   bf16 hi+lo, three products (hi*hi + hi*lo + lo*hi), FP32 accumulate.
+ * SCIR_PREC_BF16X6: tensor cores, operands split into three bf16 terms,
+ *   six products; FP32-level accuracy.
+ * SCIR_PREC_AUTO: the library picks (autotuned, accuracy <= 1e-5 normwise). */
+typedef enum scir_precision {
+    SCIR_PREC_AUTO = -1,
+    SCIR_PREC_REF_EXACT = 0,
+    SCIR_PREC_FP32 = 1,
+    SCIR_PREC_BF16X3 = 2,
+    SCIR_PREC_BF16X6 = 3
+} scir_precision;
+
+/* Arithmetic of the second-order-section recursion.
+ * SCIR_SOS_FP64_EXACT: FP64 coefficients and state, the reference DF2T
+ *   operation order without FMA (crates/scir-iir-filters/src/filter.rs:
+ *   50-61): bit-identical to the reference for f64 data.
+ * SCIR_SOS_FP64: FP64 coefficients and state with FMA.
+ * SCIR_SOS_FP32: coefficients rounded to FP32, FP32 state. */
+typedef enum scir_sos_precision {
+    SCIR_SOS_FP64_EXACT = 0,
+    SCIR_SOS_FP64 = 1,
+    SCIR_SOS_FP32 = 2
+} scir_sos_precision;
+
+/* Edge extension for sosfiltfilt (SciPy padtype). */
+typedef enum scir_padtype {
+    SCIR_PAD_NONE = 0, /* reference filtfilt: no padding, zero state       */
+    SCIR_PAD_ODD = 1   /* SciPy default: odd extension + sosfilt_zi state  */
+} scir_padtype;
+
+/* ----------------------------------------------------------------------- */
+/* Library / device layer                                                  */
+/* Replaces the per-call context and module load of the reference's CUDA   */
+/* path (crates/scir-gpu/src/lib.rs:589-622, 814-834): kernels are compiled */
+/* ahead of time for sm_103a and the primary context of the current device */
+/* is used for every call.                                                  */
+/* ----------------------------------------------------------------------- */
+
+SCIR_API int scir_abi_version(void);
+SCIR_API const char* scir_status_string(int status);
+/* Copies the calling thread's last error message (NUL-terminated). */
+SCIR_API int scir_last_error(char* buf, size_t len);
+/* Initialises per-device state for `device` (kernel attributes, SM count).
+ * Optional: every entry point initialises the current device on first use.
+ * Replaces cuda_available() / CudaCtx::create_default
+ * (crates/scir-gpu/src/lib.rs:596-616). */
+SCIR_API int scir_init(int device);
+SCIR_API int scir_device_count(int* count);
+
+/* ----------------------------------------------------------------------- */
+/* Batched FIR (device pointers, stream-ordered)                           */
+/* Replaces cuda::fir1d_batched_f32_cuda and its PTX kernel                */
+/* (crates/scir-gpu/src/lib.rs:1036-1113, 727-811).                        */
+/* ----------------------------------------------------------------------- */
+
+/* Output length of `mode` for n samples and k taps (-1 if invalid). */
+SCIR_API int64_t scir_fir_out_len(int64_t n, int64_t k, int mode);
+
+/* x: batch rows of n samples, row stride ld_x >= n; taps: k values;
+ * y: batch rows of scir_fir_out_len(n, k, mode) samples, stride ld_y. */
+SCIR_API int scir_fir_batched_f32(const float* x, int64_t ld_x, int64_t batch,
+                                  int64_t n, const float* taps, int64_t k,
+                                  int mode, int precision, float* y,
+                                  int64_t ld_y, void* stream);
+
+/* ----------------------------------------------------------------------- */
+/* Ragged batched FIR: signals of different lengths and tap counts in one  */
+/* persistent launch.  No reference counterpart exists (the reference API  */
+/* takes one shared tap vector, crates/scir-gpu/src/lib.rs:1134); this is  */
+/* the ragged extension of fir1d_batched_f32.                               */
+/* ----------------------------------------------------------------------- */
+
+typedef struct scir_ragged_desc {
+    int64_t x_off;    /* first input sample of the signal in x            */
+    int64_t n;        /* input samples                                    */
+    int64_t taps_off; /* first tap of the signal in taps                  */
+    int64_t k;        /* taps                                             */
+    int64_t y_off;    /* first output sample in y (scir_fir_out_len long) */
+} scir_ragged_desc;
+
+typedef struct scir_ragged_plan scir_ragged_plan;
+
+/* Builds a launch plan from a HOST descriptor table: validates every entry,
+ * splits signals into work tiles, orders them longest-first and uploads the
+ * tile table to the device.  `precision` may be SCIR_PREC_AUTO. */
+SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count,
+                                     int mode, int precision,
+                                     scir_ragged_plan** plan);
+SCIR_API int scir_ragged_plan_destroy(scir_ragged_plan* plan);
+/* Number of tiles and algorithmic multiply-adds of the plan. */
+SCIR_API int scir_ragged_plan_stats(const scir_ragged_plan* plan,
+                                    int64_t* tiles, double* macs,
+                                    int64_t* samples_in);
+/* One persistent launch over every tile of the plan (graph-capturable:
+ * no allocation, no host synchronisation). */
+SCIR_API int scir_fir_ragged_f32(const scir_ragged_plan* plan, const float* x,
+                                 const float* taps, float* y, void* stream);
+
+/* ----------------------------------------------------------------------- */
+/* Polyphase upfirdn / resample_poly (device pointers, stream-ordered)     */
+/* Replaces scir_signal::resample_poly (crates/scir-signal/src/lib.rs:     */
+/* 313-362), generalised to any rates as scipy.signal.upfirdn /           */
+/* resample_poly.                                                          */
+/* ----------------------------------------------------------------------- */
+
+/* scipy.signal.upfirdn output length: ceil(((n-1)*up + kh) / down). */
+SCIR_API int64_t scir_upfirdn_out_len(int64_t kh, int64_t n, int up, int down);
+/* y[m] = sum_j h[j] * u[m*down - j], u = x zero-stuffed by up. */
+SCIR_API int scir_upfirdn_f32(const float* x, int64_t ld_x, int64_t batch,
+                              int64_t n, const float* h, int64_t kh, int up,
+                              int down, int precision, float* y, int64_t ld_y,
+                              void* stream);
+
+/* resample_poly output length: ceil(n*up/down) after gcd reduction. */
+SCIR_API int64_t scir_resample_poly_out_len(int64_t n, int up, int down);
+
+/* Default anti-aliasing design for resample_poly, computed on the host in
+ * FP64 and already multiplied by the reduced `up`:
+ *   design 0 (SciPy): firwin(2*10*max(up,down)+1, 1/max, ('kaiser', 5.0));
+ *   design 1 (reference): the reference's baked 2/3 table, which is
+ *   firwin(31, 1/3, 'hamming') * 2 (crates/scir-signal/src/lib.rs:315-347);
+ *   only up/down = 2/3 (after reduction) is accepted.
+ * Writes at most `cap` taps to h (host) and the count to *kh. */
+SCIR_API int scir_resample_poly_default_taps(int up, int down, int design,
+                                             double* h, int64_t cap,
+                                             int64_t* kh);
+
+/* resample_poly with zero-padded edges: after gcd reduction of up/down,
+ * y[m] = sum_j h[j] * u[(kh-1)/2 + m*down - j] for m < ceil(n*up/down).
+ * h (device, kh taps) must already include the gain `up`; h == NULL selects
+ * scir_resample_poly_default_taps(design 0).  up == down: y = x. */
+SCIR_API int scir_resample_poly_f32(const float* x, int64_t ld_x, int64_t batch,
+                                    int64_t n, int up, int down, const float* h,
+                                    int64_t kh, int precision, float* y,
+                                    int64_t ld_y, void* stream);
+
+/* ----------------------------------------------------------------------- */
+/* Second-order sections (device pointers, stream-ordered)                 */
+/* Replaces scir_signal::sosfilt / filtfilt (crates/scir-signal/src/lib.rs:*/
+/* 260-291) over DirectForm2Transposed (crates/scir-iir-filters/src/       */
+/* filter.rs:50-61).  sos is [nsec][6] = b0 b1 b2 a0 a1 a2, the layout of  */
+/* #[repr(C)] SosCoeffs (crates/scir-iir-filters/src/sos.rs:49-66); a0 is  */
+/* taken as 1 and not read, as in the reference.                            */
+/* ----------------------------------------------------------------------- */
+
+#define SCIR_SOS_MAX_SECTIONS 32
+
+/* x, y: batch rows of n samples (f32, or f64 for the _f64 variant);
+ * sos: HOST pointer, [nsec][6] f64 (copied into kernel parameters);
+ * zi: optional DEVICE [batch][nsec][2] f64 initial DF2T state (s1, s2);
+ * zf: optional DEVICE [batch][nsec][2] f64 final state. */
+SCIR_API int scir_sosfilt_f32(const float* x, int64_t ld_x, int64_t batch,
+                              int64_t n, const double* sos, int nsec,
+                              const double* zi, double* zf, int precision,
+                              float* y, int64_t ld_y, void* stream);
+SCIR_API int scir_sosfilt_f64(const double* x, int64_t ld_x, int64_t batch,
+                              int64_t n, const double* sos, int nsec,
+                              const double* zi, double* zf, int precision,
+                              double* y, int64_t ld_y, void* stream);
+
+/* SciPy sosfilt_zi for a HOST sos: zi[nsec][2] (host). */
+SCIR_API int scir_sosfilt_zi(const double* sos, int nsec, double* zi);
+/* SciPy's default filtfilt edge: 3*(2*nsec+1 - min(#b2==0, #a2==0)). */
+SCIR_API int64_t scir_sosfiltfilt_default_padlen(const double* sos, int nsec);
+
+/* Forward-backward filtering.  SCIR_PAD_NONE is the reference filtfilt
+ * (zero state both ways, crates/scir-signal/src/lib.rs:278-291);
+ * SCIR_PAD_ODD is scipy.signal.sosfiltfilt (odd extension of padlen samples
+ * each side, padlen < 0 = default, initial states sosfilt_zi * edge value).
+ * y may alias x. */
+SCIR_API int scir_sosfiltfilt_f32(const float* x, int64_t ld_x, int64_t batch,
+                                  int64_t n, const double* sos, int nsec,
+                                  int padtype, int64_t padlen, int precision,
+                                  float* y, int64_t ld_y, void* stream);
+SCIR_API int scir_sosfiltfilt_f64(const double* x, int64_t ld_x, int64_t batch,
+                                  int64_t n, const double* sos, int nsec,
+                                  int padtype, int64_t padlen, int precision,
+                                  double* y, int64_t ld_y, void* stream);
+
+/* ----------------------------------------------------------------------- */
+/* Host-buffer entry points with the reference's signatures (synchronous). */
+/* ----------------------------------------------------------------------- */
+
+/* crates/scir-gpu/src/lib.rs:1036 fir1d_batched_f32_cuda(x: &Array2<f32>,
+ * taps: &Array1<f32>) -> Result<Array2<f32>, GpuError>; x is b x n
+ * row-major, y (b x n) is caller-allocated.  Uses SCIR_PREC_REF_EXACT, so
+ * y is bit-identical to scir_gpu::fir1d_batched_f32 (lib.rs:1134). */
+SCIR_API int scir_fir1d_batched_f32_cuda(const float* x, size_t b, size_t n,
+                                         const float* taps, size_t k, float* y);
+
+/* Generalised host-buffer FIR (any mode/precision), chunked over rows and
+ * pipelined H2D / kernel / D2H on library streams. */
+SCIR_API int scir_fir_batched_f32_host(const float* x, int64_t batch, int64_t n,
+                                       const float* taps, int64_t k, int mode,
+                                       int precision, float* y);
+
+/* crates/scir-signal/src/lib.rs:260 sosfilt(sos: &Sos, x: &Array1<f64>)
+ * -> Array1<f64>; batch rows allowed.  Uses SCIR_SOS_FP64_EXACT. */
+SCIR_API int scir_sosfilt_f64_host(const double* sos, int nsec, const double* x,
+                                   size_t batch, size_t n, double* y);
+/* crates/scir-signal/src/lib.rs:278 filtfilt(sos, x) (no padding). */
+SCIR_API int scir_filtfilt_f64_host(const double* sos, int nsec, const double* x,
+                                    size_t batch, size_t n, double* y);
+/* crates/scir-signal/src/lib.rs:313 resample_poly(x, up, down) with the
+ * reference's design (only 2/3 accepted, as the reference asserts); y holds
+ * scir_resample_poly_out_len(n, 2, 3) values per row. */
+SCIR_API int scir_resample_poly_f64_host(const double* x, size_t batch,
+                                         size_t n, size_t up, size_t down,
+                                         double* y);
+/* Host-buffer resample_poly on f32 rows with the SciPy design (h == NULL)
+ * or explicit host taps, pipelined like scir_fir_batched_f32_host. */
+SCIR_API int scir_resample_poly_f32_host(const float* x, int64_t batch,
+                                         int64_t n, int up, int down,
+                                         const float* h, int64_t kh,
+                                         int precision, float* y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SCIR_GB300_H */

@@ -1,0 +1,69 @@
+// Launcher interfaces shared between the C-ABI layer and the kernel files.
+#pragma once
+
+#include "common.cuh"
+
+namespace scir {
+
+// A batched FIR request in correlation form:
+//   y[row][o] = sum_{m<k} c[m] * x[row][o + s + m],  x = 0 outside [0, n),
+// with c[m] = taps[reverse ? k-1-m : m] and o in [0, n_out).
+struct FirArgs {
+    const float* x;
+    int64_t ld_x, batch, n;
+    const float* taps;
+    int64_t k;
+    int reverse;
+    int64_t s;
+    float* y;
+    int64_t ld_y, n_out;
+};
+
+// Fills reverse / s / n_out from a scir_fir_mode; returns a status.
+int fir_geometry(int64_t n, int64_t k, int mode, int* reverse, int64_t* s, int64_t* n_out);
+
+int launch_fir_simt(const FirArgs& a, bool exact, cudaStream_t st);
+// Tensor-core (tcgen05) FIR with split-bf16 operands; terms = 2 (BF16X3) or 3 (BF16X6).
+int launch_fir_tc(const FirArgs& a, int terms, cudaStream_t st);
+bool fir_tc_supported(const FirArgs& a);
+
+// Polyphase FIR: y[m] = sum_q h[ph + q*up] * x[base - q],
+// t = m*down + off, ph = t mod up, base = t div up, m in [0, n_out).
+struct PolyArgs {
+    const float* x;
+    int64_t ld_x, batch, n;
+    const float* h;
+    int64_t kh;
+    int up, down;
+    int64_t off;
+    float* y;
+    int64_t ld_y, n_out;
+};
+int launch_poly_simt(const PolyArgs& a, cudaStream_t st);
+int launch_poly_tc(const PolyArgs& a, int terms, cudaStream_t st);
+bool poly_tc_supported(const PolyArgs& a);
+
+// Second-order sections.
+struct SosCoef {
+    double c[SCIR_SOS_MAX_SECTIONS][5];  // b0 b1 b2 a1 a2 (a0 taken as 1); unused = identity
+    float cf[SCIR_SOS_MAX_SECTIONS][5];  // the same rounded to FP32
+    double zi[SCIR_SOS_MAX_SECTIONS][2]; // sosfilt_zi (filtfilt with padding)
+    int nsec;
+};
+template <typename T>
+int launch_sosfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const SosCoef& c,
+                   const double* zi, double* zf, int precision, T* y, int64_t ld_y,
+                   cudaStream_t st);
+template <typename T>
+int launch_sosfiltfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const SosCoef& c,
+                       int64_t edge, int use_zi, int precision, T* y, int64_t ld_y,
+                       T* tail_scratch, cudaStream_t st);
+
+// Host-side FP64 design helpers (design.cpp).
+int sos_zi_host(const double* sos, int nsec, double* zi);
+int64_t sos_default_padlen(const double* sos, int nsec);
+int64_t gcd64(int64_t a, int64_t b);
+// firwin low-pass, window 0 = Hamming, 1 = Kaiser(beta); unit DC gain.
+void firwin_lowpass(int64_t numtaps, double cutoff, int window, double beta, double* h);
+
+}  // namespace scir

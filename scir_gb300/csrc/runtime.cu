@@ -1,0 +1,165 @@
+// Device and error layer of the library.
+//
+// The reference creates a CUDA context and JIT-loads its PTX module on every
+// call (crates/scir-gpu/src/lib.rs:589-622, 814-834) and reports failures as
+// GpuError (lib.rs:58-63).  Here kernels are compiled ahead of time for
+// sm_103a, the runtime's primary context of the current device is used, the
+// per-device facts are cached once, and errors are status codes plus a
+// thread-local message.
+#include "common.cuh"
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+namespace scir {
+
+namespace {
+thread_local char g_last_error[1024] = {0};
+
+constexpr int kMaxDevices = 64;
+std::mutex g_dev_mutex;
+DeviceInfo g_dev[kMaxDevices];
+bool g_dev_ready[kMaxDevices] = {false};
+
+// A trivial kernel whose presence proves an sm_103 image was loaded.
+__global__ void probe_kernel() {}
+}  // namespace
+
+int set_error(int status, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+    return status;
+}
+
+void clear_error() { g_last_error[0] = 0; }
+
+static int init_device_locked(int dev) {
+    DeviceInfo& d = g_dev[dev];
+    cudaDeviceProp prop;
+    SCIR_CUDA_TRY(cudaGetDeviceProperties(&prop, dev));
+    d.device = dev;
+    d.sm_count = prop.multiProcessorCount;
+    d.max_smem_optin = (int)prop.sharedMemPerBlockOptin;
+    d.cc_major = prop.major;
+    d.cc_minor = prop.minor;
+    d.l2_bytes = prop.l2CacheSize;
+    cudaFuncAttributes attr;
+    cudaError_t e = cudaFuncGetAttributes(&attr, probe_kernel);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(SCIR_ERR_NO_DEVICE,
+                         "device %d (sm_%d%d) has no kernel image in this library "
+                         "(built for sm_103a): %s",
+                         dev, prop.major, prop.minor, cudaGetErrorString(e));
+    }
+    g_dev_ready[dev] = true;
+    return SCIR_OK;
+}
+
+int current_device(const DeviceInfo** info) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(SCIR_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+    }
+    if (dev < 0 || dev >= kMaxDevices)
+        return set_error(SCIR_ERR_NO_DEVICE, "device ordinal %d out of range", dev);
+    if (!g_dev_ready[dev]) {
+        std::lock_guard<std::mutex> lk(g_dev_mutex);
+        if (!g_dev_ready[dev]) {
+            int rc = init_device_locked(dev);
+            if (rc != SCIR_OK) return rc;
+        }
+    }
+    *info = &g_dev[dev];
+    return SCIR_OK;
+}
+
+int upload_sync(void* dst, const void* src, size_t bytes) {
+    if (bytes == 0) return SCIR_OK;
+    static std::mutex mu;
+    static cudaStream_t streams[kMaxDevices] = {};
+    int dev = 0;
+    SCIR_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return set_error(SCIR_ERR_NO_DEVICE, "bad device %d", dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if (!streams[dev]) SCIR_CUDA_TRY(cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking));
+    SCIR_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, streams[dev]));
+    SCIR_CUDA_TRY(cudaStreamSynchronize(streams[dev]));
+    return SCIR_OK;
+}
+
+int scratch_alloc(void** p, size_t bytes, cudaStream_t stream) {
+    *p = nullptr;
+    if (bytes == 0) return SCIR_OK;
+    cudaError_t e = cudaMallocAsync(p, bytes, stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(e == cudaErrorMemoryAllocation ? SCIR_ERR_OOM : SCIR_ERR_CUDA,
+                         "scratch allocation of %zu bytes failed: %s", bytes,
+                         cudaGetErrorString(e));
+    }
+    return SCIR_OK;
+}
+
+void scratch_free(void* p, cudaStream_t stream) {
+    if (p) cudaFreeAsync(p, stream);
+}
+
+}  // namespace scir
+
+extern "C" {
+
+SCIR_API int scir_abi_version(void) { return SCIR_GB300_ABI_VERSION; }
+
+SCIR_API const char* scir_status_string(int status) {
+    switch (status) {
+    case SCIR_OK: return "ok";
+    case SCIR_ERR_INVALID_ARG: return "invalid argument";
+    case SCIR_ERR_SHAPE: return "shape mismatch";
+    case SCIR_ERR_ALIGN: return "misaligned pointer or stride";
+    case SCIR_ERR_OOM: return "out of memory";
+    case SCIR_ERR_CUDA: return "CUDA error";
+    case SCIR_ERR_TIMEOUT: return "device wait timed out";
+    case SCIR_ERR_UNSUPPORTED: return "unsupported";
+    case SCIR_ERR_NO_DEVICE: return "no usable CUDA device";
+    default: return "unknown status";
+    }
+}
+
+SCIR_API int scir_last_error(char* buf, size_t len) {
+    if (!buf || len == 0) return SCIR_ERR_INVALID_ARG;
+    strncpy(buf, scir::g_last_error, len - 1);
+    buf[len - 1] = 0;
+    return SCIR_OK;
+}
+
+SCIR_API int scir_device_count(int* count) {
+    if (!count) return scir::set_error(SCIR_ERR_INVALID_ARG, "count is NULL");
+    *count = 0;
+    cudaError_t e = cudaGetDeviceCount(count);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *count = 0;
+        return scir::set_error(SCIR_ERR_NO_DEVICE, "cudaGetDeviceCount: %s", cudaGetErrorString(e));
+    }
+    return SCIR_OK;
+}
+
+SCIR_API int scir_init(int device) {
+    int count = 0;
+    int rc = scir_device_count(&count);
+    if (rc != SCIR_OK) return rc;
+    if (device < 0 || device >= count)
+        return scir::set_error(SCIR_ERR_INVALID_ARG, "device %d not in [0, %d)", device, count);
+    SCIR_CUDA_TRY(cudaSetDevice(device));
+    const scir::DeviceInfo* info = nullptr;
+    return scir::current_device(&info);
+}
+
+}  // extern "C"

@@ -1,0 +1,132 @@
+"""C-ABI surface and host-side logic that needs no GPU: every symbol the
+header declares is exported, sizes/geometry agree with the oracle and SciPy,
+the FP64 design helpers match SciPy, and argument validation rejects bad
+calls before any device work."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+import scipy.signal as ss
+
+import oracle as O
+import scir_gb300 as S
+from scir_gb300 import _native
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "scir_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"SCIR_API\s+[\w\s\*]+?\b(scir_\w+)\s*\(", text)))
+
+
+def test_header_symbols_exported_and_bound():
+    L = S.load()
+    syms = declared_symbols()
+    assert len(syms) >= 25
+    for name in syms:
+        assert hasattr(L, name), f"{name} declared in the header but not exported"
+        assert name in _native.SIGNATURES, f"{name} has no ctypes signature"
+    assert set(_native.SIGNATURES) == set(syms)
+    assert L.scir_abi_version() == 1
+
+
+def test_status_strings():
+    assert S.status_string(0) == "ok"
+    assert "shape" in S.status_string(2)
+    assert S.status_string(99) == "unknown status"
+
+
+@pytest.mark.parametrize("n,k", [(10, 3), (3, 10), (1, 1), (65536, 63), (0, 4)])
+def test_fir_out_len(n, k):
+    for mode in range(4):
+        exp = O.fir_out_len(n, k, mode) if n > 0 or mode < 2 else None
+        got = S.load().scir_fir_out_len(n, k, mode)
+        if mode == 3 and n < k:
+            assert got == -1
+        elif exp is not None:
+            assert got == exp
+
+
+@pytest.mark.parametrize("kh,n,up,down", [(3201, 1048576, 160, 147), (31, 32, 2, 3), (9, 5, 1, 4),
+                                          (22, 77, 5, 1)])
+def test_poly_lengths(kh, n, up, down):
+    assert S.upfirdn_out_len(kh, n, up, down) == O.lib().orc_upfirdn_out_len(kh, n, up, down)
+    assert S.resample_poly_out_len(n, up, down) == O.resample_poly_out_len(n, up, down)
+
+
+def test_resample_cfg_output_length():
+    # 256 x 1,048,576 at 160/147 gives 1,141,308 outputs per channel
+    assert S.resample_poly_out_len(1048576, 160, 147) == 1141308
+
+
+def test_reference_design_is_hamming_31():
+    h = S.resample_poly_default_taps(2, 3, design=1)
+    np.testing.assert_allclose(h, ss.firwin(31, 1 / 3, window="hamming") * 2, atol=1e-16, rtol=1e-13)
+    assert h.size == 31
+
+
+@pytest.mark.parametrize("up,down", [(160, 147), (2, 3), (3, 2), (1, 5), (4, 6)])
+def test_scipy_default_design(up, down):
+    import math
+    g = math.gcd(up, down)
+    u, d = up // g, down // g
+    mr = max(u, d)
+    ref = ss.firwin(2 * 10 * mr + 1, 1.0 / mr, window=("kaiser", 5.0)) * u
+    h = S.resample_poly_default_taps(up, down, design=0)
+    np.testing.assert_allclose(h, ref, atol=1e-15, rtol=1e-11)
+
+
+def test_reference_design_rejects_other_rates():
+    with pytest.raises(S.GpuError) as ei:
+        S.resample_poly_default_taps(160, 147, design=1)
+    assert ei.value.status == S.ERR_UNSUPPORTED
+
+
+def test_sosfilt_zi_and_padlen():
+    for sos in [ss.butter(8, [0.001, 0.002], btype="bandpass", output="sos"),
+                ss.butter(4, 0.2, output="sos"), ss.cheby1(5, 1, 0.3, output="sos")]:
+        np.testing.assert_allclose(S.sosfilt_zi(sos), ss.sosfilt_zi(sos), rtol=1e-12, atol=1e-14)
+        assert S.sosfiltfilt_default_padlen(sos) == O.sosfiltfilt_default_padlen(sos)
+
+
+def test_validation_before_device():
+    L = S.load()
+    f = ctypes.c_void_p(16)
+    # VALID with n < k
+    assert L.scir_fir_batched_f32(f, 4, 1, 4, f, 8, 3, 1, f, 4, None) == S.ERR_SHAPE
+    # row stride shorter than the row
+    assert L.scir_fir_batched_f32(f, 3, 2, 4, f, 2, 1, 1, f, 4, None) == S.ERR_SHAPE
+    # null taps
+    assert L.scir_fir_batched_f32(f, 4, 1, 4, None, 2, 1, 1, f, 4, None) == S.ERR_INVALID_ARG
+    # unknown mode / precision
+    assert L.scir_fir_batched_f32(f, 4, 1, 4, f, 2, 9, 1, f, 4, None) == S.ERR_INVALID_ARG
+    assert L.scir_fir_batched_f32(f, 4, 1, 4, f, 2, 1, 7, f, 4, None) == S.ERR_INVALID_ARG
+    # upfirdn with up = 0
+    assert L.scir_upfirdn_f32(f, 4, 1, 4, f, 3, 0, 1, 1, f, 8, None) == S.ERR_INVALID_ARG
+    assert "up and down" in S.last_error()
+    # sos section count out of range
+    sos = np.zeros((40, 6))
+    assert L.scir_sosfilt_f32(f, 4, 1, 4, sos.ctypes.data, 40, None, None, 1, f, 4, None) \
+        == S.ERR_INVALID_ARG
+    # the ragged plan rejects a descriptor with k = 0 before any upload
+    with pytest.raises(S.GpuError):
+        S.RaggedPlan([10, 20], [3, 0])
+
+
+def test_no_silent_cpu_path():
+    with pytest.raises(S.GpuError) as ei:
+        S.fir1d_batched_f32_auto(np.zeros((1, 4), np.float32), np.ones(3, np.float32), S.Device.Cpu)
+    assert ei.value.kind == "BackendUnavailable"
+
+
+def test_no_device_is_an_error_not_a_fallback():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    with pytest.raises(S.GpuError) as ei:
+        S.fir1d_batched_f32_cuda(np.zeros((1, 4), np.float32), np.ones(3, np.float32))
+    assert ei.value.status in (S.ERR_NO_DEVICE, S.ERR_CUDA)

@@ -1,0 +1,128 @@
+"""Batched FIR on the GPU through the C ABI vs the oracle.
+
+Tolerances: REF_EXACT is compared bit for bit with the f32 restatement of the
+reference loop; FP32 (FMA, different summation order) must be within 1e-5
+normwise (max|y - y64| / max|y64|) of the FP64 oracle on the same
+f32-rounded inputs."""
+import numpy as np
+import pytest
+import scipy.signal as ss
+
+import oracle as O
+import scir_gb300 as S
+from conftest import normwise_err
+
+pytestmark = pytest.mark.gpu
+TOL_FP32 = 1e-5
+
+
+def _dev(a, cuda):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+
+
+def test_known_answer_host_api(cuda):
+    # crates/scir-gpu/src/lib.rs:1300-1323 cuda_fir1d_batched_f32_parity_small
+    x = np.array([[1.0, 2.0, 3.0, 4.0], [0.5, 0.0, -0.5, -1.0]], np.float32)
+    taps = np.array([0.25, 0.5, 0.25], np.float32)
+    y = S.fir1d_batched_f32_cuda(x, taps)
+    np.testing.assert_allclose(y, [[0.25, 1, 2, 3], [0.125, 0.25, 0, -0.5]], atol=1e-7)
+    assert np.array_equal(y, O.fir1d_batched_f32(x, taps))
+    assert np.array_equal(S.fir1d_batched_f32_auto(x, taps, S.Device.Cuda), y)
+
+
+@pytest.mark.parametrize("b,n,k", [(3, 1000, 5), (2, 100, 63), (4, 5000, 300), (2, 10, 20),
+                                   (1, 1, 1), (2, 9000, 5000), (5, 4097, 128), (1, 70000, 17)])
+def test_ref_exact_is_bit_identical(cuda, b, n, k):
+    rng = np.random.default_rng(b * 7919 + n + k)
+    x = rng.uniform(-1, 1, (b, n)).astype(np.float32)
+    taps = rng.standard_normal(k).astype(np.float32)  # asymmetric: pins orientation
+    ref = O.fir1d_batched_f32(x, taps)
+    y = S.fir_batched(_dev(x, cuda), _dev(taps, cuda), S.FirMode.REF_CORR,
+                      S.Precision.REF_EXACT).cpu().numpy()
+    assert np.array_equal(y, ref)
+    assert np.array_equal(S.fir1d_batched_f32_cuda(x, taps), ref)
+
+
+@pytest.mark.parametrize("mode", list(S.FirMode))
+@pytest.mark.parametrize("b,n,k", [(3, 3000, 63), (2, 20000, 700), (2, 500, 9)])
+def test_fp32_modes_vs_fp64(cuda, mode, b, n, k):
+    rng = np.random.default_rng(n + k + int(mode))
+    x = rng.uniform(-1, 1, (b, n)).astype(np.float32)
+    taps = rng.standard_normal(k).astype(np.float32)
+    ref = O.fir_mode_f64(x.astype(np.float64), taps.astype(np.float64), int(mode))
+    y = S.fir_batched(_dev(x, cuda), _dev(taps, cuda), mode, S.Precision.FP32).cpu().numpy()
+    assert y.shape == ref.shape
+    assert normwise_err(y, ref) < TOL_FP32
+
+
+def test_strided_rows_and_out(cuda):
+    import torch
+    rng = np.random.default_rng(11)
+    big = rng.uniform(-1, 1, (4, 3000)).astype(np.float32)
+    taps = rng.standard_normal(31).astype(np.float32)
+    xd = _dev(big, cuda)[:, 100:2100]            # ld = 3000, n = 2000
+    out = torch.zeros((4, 2500), device=cuda)[:, :2000]
+    S.fir_batched(xd, _dev(taps, cuda), S.FirMode.REF_CORR, S.Precision.REF_EXACT, out=out)
+    ref = O.fir1d_batched_f32(np.ascontiguousarray(big[:, 100:2100]), taps)
+    assert np.array_equal(out.cpu().numpy(), ref)
+
+
+def test_cfg1_full_size(cuda):
+    # 64 channels x 65,536 samples U[-1,1), 63-tap Hamming low-pass at 0.2 Nyquist
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1, 1, (64, 65536)).astype(np.float32)
+    taps = ss.firwin(63, 0.2, window="hamming").astype(np.float32)
+    xd, td = _dev(x, cuda), _dev(taps, cuda)
+    ref32 = O.fir1d_batched_f32(x, taps)
+    y = S.fir_batched(xd, td, S.FirMode.REF_CORR, S.Precision.REF_EXACT).cpu().numpy()
+    assert np.array_equal(y, ref32)
+    x64, t64 = x.astype(np.float64), taps.astype(np.float64)
+    for mode in (S.FirMode.FULL, S.FirMode.VALID):
+        ref = O.fir_mode_f64(x64[:8], t64, int(mode))
+        yd = S.fir_batched(xd, td, mode, S.Precision.FP32).cpu().numpy()
+        assert yd.shape == (64, S.fir_out_len(65536, 63, mode))
+        assert normwise_err(yd[:8], ref) < TOL_FP32
+
+
+def test_cfg3_long_taps_fp32(cuda):
+    # 4,095-tap Kaiser(8.6) band-pass 0.1-0.3 Nyquist on sinusoid mixtures, 2 channels
+    rng = np.random.default_rng(0)
+    n = 65536
+    t = np.arange(n)
+    x = np.zeros((2, n))
+    for c in range(2):
+        f = rng.uniform(0, 0.5, 32)
+        ph = rng.uniform(0, 2 * np.pi, 32)
+        x[c] = np.sum(np.sin(2 * np.pi * f[:, None] * t[None, :] + ph[:, None]), 0) / 32
+        x[c] += rng.normal(0, 0.1, n)
+    x = x.astype(np.float32)
+    taps = ss.firwin(4095, [0.1, 0.3], window=("kaiser", 8.6), pass_zero=False).astype(np.float32)
+    ref = O.fir_mode_f64(x.astype(np.float64), taps.astype(np.float64), int(S.FirMode.LFILTER))
+    y = S.fir_batched(_dev(x, cuda), _dev(taps, cuda), S.FirMode.LFILTER, S.Precision.FP32)
+    assert normwise_err(y.cpu().numpy(), ref) < TOL_FP32
+
+
+def test_empty_taps_and_empty_batch(cuda):
+    import torch
+    x = _dev(np.ones((2, 5), np.float32), cuda)
+    y = S.fir_batched(x, torch.empty(0, device=cuda), S.FirMode.REF_CORR, S.Precision.FP32)
+    assert np.array_equal(y.cpu().numpy(), np.zeros((2, 5), np.float32))
+    e = torch.empty((0, 7), device=cuda)
+    assert S.fir_batched(e, _dev(np.ones(3, np.float32), cuda)).shape == (0, 7)
+
+
+def test_shape_errors(cuda):
+    x = _dev(np.ones((1, 4), np.float32), cuda)
+    with pytest.raises(S.GpuError) as ei:
+        S.fir_batched(x, _dev(np.ones(8, np.float32), cuda), S.FirMode.VALID)
+    assert ei.value.kind == "ShapeMismatch"
+
+
+def test_host_pipeline_many_chunks(cuda):
+    # enough rows that the host layer splits into several pipelined chunks
+    rng = np.random.default_rng(12)
+    x = rng.uniform(-1, 1, (600, 40000)).astype(np.float32)
+    taps = rng.standard_normal(15).astype(np.float32)
+    y = S.fir_batched_host(x, taps, S.FirMode.REF_CORR, S.Precision.REF_EXACT)
+    assert np.array_equal(y[::37], O.fir1d_batched_f32(x[::37], taps))

@@ -1,0 +1,165 @@
+"""The oracle is pinned before it is trusted: every check here compares the C
+restatement with the reference's own golden vectors, known answers and
+fixtures (CPU only)."""
+import numpy as np
+import pytest
+import scipy.signal as ss
+
+import oracle as O
+
+from conftest import normwise_err
+
+
+# crates/scir-gpu/src/lib.rs:1249-1261 fir_batched_matches_naive_f32
+def test_fir_known_answer():
+    x = np.array([[1.0, 2.0, 3.0, 4.0], [0.5, 0.0, -0.5, -1.0]], np.float32)
+    taps = np.array([0.25, 0.5, 0.25], np.float32)
+    y = O.fir1d_batched_f32(x, taps)
+    np.testing.assert_allclose(y[0], [0.25, 1.0, 2.0, 3.0], atol=1e-7, rtol=1e-7)
+    np.testing.assert_allclose(y[1], [0.125, 0.25, 0.0, -0.5], atol=1e-7, rtol=1e-7)
+
+
+# crates/scir-gpu/src/lib.rs:1263-1298 fir_batched_random_f64: asymmetric taps
+# 1/(i+1) pin the orientation (the reference test is unseeded; seeds here)
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_fir_orientation_asymmetric(seed):
+    rng = np.random.default_rng(seed)
+    x = rng.random((3, 32)) * 2 - 1
+    taps = 1.0 / (np.arange(5) + 1.0)
+    y = O.fir1d_batched_f64(x, taps)
+    ref = np.zeros_like(x)
+    for b in range(3):
+        for i in range(32):
+            acc = 0.0
+            for t, xi in enumerate(range(i, max(i + 1 - 5, 0) - 1, -1)):
+                acc += taps[5 - 1 - t] * x[b, xi]
+            ref[b, i] = acc
+    np.testing.assert_allclose(y, ref, atol=1e-12, rtol=1e-12)
+    # reversed-tap lfilter, not lfilter(taps)
+    np.testing.assert_allclose(y, ss.lfilter(taps[::-1], 1, x, axis=1), atol=1e-12)
+    assert np.max(np.abs(y - ss.lfilter(taps, 1, x, axis=1))) > 1e-3
+
+
+def test_fir_f32_restatement_is_sequential_f32():
+    # the f32 loop accumulates in f32 without FMA: reproduce it in numpy float32
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-1, 1, (2, 200)).astype(np.float32)
+    taps = rng.standard_normal(17).astype(np.float32)
+    y = O.fir1d_batched_f32(x, taps)
+    k = taps.size
+    ref = np.zeros_like(x)
+    for b in range(2):
+        for i in range(200):
+            acc = np.float32(0)
+            t = 0
+            for xi in range(i, max(i + 1 - k, 0) - 1, -1):
+                acc = np.float32(acc + np.float32(taps[k - 1 - t] * x[b, xi]))
+                t += 1
+            ref[b, i] = acc
+    assert np.array_equal(y, ref)
+
+
+@pytest.mark.parametrize("mode", [O.MODE_REF, O.MODE_LFILTER, O.MODE_FULL, O.MODE_VALID])
+def test_fir_modes_vs_numpy(mode):
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal((3, 100))
+    taps = rng.standard_normal(9)
+    y = O.fir_mode_f64(x, taps, mode)
+    if mode == O.MODE_REF:
+        ref = ss.lfilter(taps[::-1], 1, x, axis=1)
+    elif mode == O.MODE_LFILTER:
+        ref = ss.lfilter(taps, 1, x, axis=1)
+    else:
+        ref = np.array([np.convolve(r, taps, "full" if mode == O.MODE_FULL else "valid") for r in x])
+    np.testing.assert_allclose(y, ref, atol=1e-12)
+
+
+# crates/scir-iir-filters/src/filter.rs:287-428: DF2T vs SciPy at 1e-12 on the
+# strain-gauge recording, four butter(5) designs
+@pytest.mark.parametrize("case", ["low_pass", "high_pass", "band_pass", "band_stop"])
+def test_df2t_strain_golden(golden_strain, case):
+    y = O.sosfilt_f64(golden_strain[f"sos_{case}"], golden_strain["x"])[0]
+    np.testing.assert_allclose(y, golden_strain[f"y_{case}"], atol=1e-12, rtol=0)
+
+
+# crates/scir-signal/src/lib.rs:410-425, 638-653 (atol = rtol = 1e-6)
+def test_sosfilt_and_filtfilt_fixtures(golden_signal):
+    f = golden_signal
+    y = O.sosfilt_f64(f["butter_sos"], f["sosfilt_input"])[0]
+    np.testing.assert_allclose(y, f["sosfilt_output"], atol=1e-6, rtol=1e-6)
+    y = O.filtfilt_ref_f64(f["butter_sos"], f["sosfilt_input"])[0]
+    np.testing.assert_allclose(y, f["filtfilt_output"], atol=1e-6, rtol=1e-6)
+    for name in ["cheby", "bessel", "butter_hp", "cheby_hp", "bessel_hp", "notch",
+                 "bessel_lp_delay", "bessel_lp_mag"]:
+        y = O.sosfilt_f64(f[f"{name}_sos"], f["sosfilt_input"])[0]
+        np.testing.assert_allclose(y, f[f"{name}_output"], atol=1e-12, rtol=1e-12)
+
+
+# crates/scir-signal/src/lib.rs:655-668: the reference resample_poly(2,3)
+# (31-tap Hamming design) matches SciPy's 61-tap default only to 2e-2
+def test_resample_reference_fixture(golden_signal):
+    h = ss.firwin(31, 1.0 / 3.0, window="hamming") * 2
+    y = O.resample_poly_ref_f64(golden_signal["sosfilt_input"], 2, 3, h)[0]
+    exp = golden_signal["resample_poly_output"]
+    assert y.shape == exp.shape
+    np.testing.assert_allclose(y, exp, atol=2e-2, rtol=1e-6)
+    assert np.max(np.abs(y - exp)) > 1e-3  # really a different design
+
+
+def test_resample_fast_equals_reference_loop():
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((2, 300))
+    for up, down, kh in [(2, 3, 31), (3, 2, 15), (160, 147, 3201), (5, 1, 21)]:
+        h = rng.standard_normal(kh)
+        a = O.resample_poly_ref_f64(x[:, :120], up, down, h)
+        b = O.resample_poly_fast_f64(x[:, :120], up, down, h)
+        assert a.shape == b.shape
+        np.testing.assert_allclose(a, b, atol=1e-12)
+
+
+@pytest.mark.parametrize("up,down", [(160, 147), (2, 3), (3, 2), (1, 4), (7, 1)])
+def test_resample_matches_scipy(up, down):
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal((2, 4000))
+    mr = max(up, down)
+    h = ss.firwin(2 * 10 * mr + 1, 1.0 / mr, window=("kaiser", 5.0)) * up
+    y = O.resample_poly_fast_f64(x, up, down, h)
+    ref = ss.resample_poly(x, up, down, axis=1)
+    np.testing.assert_allclose(y, ref, atol=1e-12)
+
+
+@pytest.mark.parametrize("up,down,kh,n", [(3, 2, 11, 77), (1, 4, 9, 5), (5, 1, 22, 1), (7, 3, 4, 30)])
+def test_upfirdn_matches_scipy(up, down, kh, n):
+    rng = np.random.default_rng(7)
+    h = rng.standard_normal(kh)
+    x = rng.standard_normal((2, n))
+    np.testing.assert_allclose(O.upfirdn_f64(h, x, up, down), ss.upfirdn(h, x, up, down, axis=1),
+                               atol=1e-12)
+
+
+def test_sosfiltfilt_and_zi_match_scipy():
+    sos = ss.butter(8, [0.001, 0.002], btype="bandpass", output="sos")
+    np.testing.assert_allclose(O.sosfilt_zi(sos), ss.sosfilt_zi(sos), rtol=1e-12, atol=1e-14)
+    assert O.sosfiltfilt_default_padlen(sos) == 51
+    rng = np.random.default_rng(8)
+    x = rng.standard_normal((2, 6000))
+    y = O.sosfiltfilt_f64(sos, x)
+    ref = ss.sosfiltfilt(sos, x, axis=1)
+    assert normwise_err(y, ref) < 1e-12
+    y2 = O.sosfiltfilt_f64(sos, x, padlen=200)
+    assert normwise_err(y2, ss.sosfiltfilt(sos, x, axis=1, padlen=200)) < 1e-12
+
+
+def test_sosfilt_state_in_out():
+    sos = ss.butter(4, 0.2, output="sos")
+    rng = np.random.default_rng(9)
+    x = rng.standard_normal((3, 500))
+    zi = rng.standard_normal((3, sos.shape[0], 2))
+    y, zf = O.sosfilt_f64(sos, x, zi=zi, return_zf=True)
+    yr, zr = ss.sosfilt(sos, x, axis=1, zi=np.transpose(zi, (1, 0, 2)))
+    np.testing.assert_allclose(y, yr, atol=1e-12)
+    np.testing.assert_allclose(zf, np.transpose(zr, (1, 0, 2)), atol=1e-12)
+    # chunked filtering with carried state equals one pass
+    y1, z1 = O.sosfilt_f64(sos, x[:, :200], return_zf=True)
+    y2 = O.sosfilt_f64(sos, x[:, 200:], zi=z1)
+    np.testing.assert_allclose(np.concatenate([y1, y2], 1), O.sosfilt_f64(sos, x), atol=1e-12)

@@ -1,0 +1,99 @@
+"""Polyphase upfirdn / resample_poly on the GPU vs the oracle.
+
+FP32 paths must be within 1e-5 normwise of the FP64 oracle on the same
+f32-rounded inputs and taps; the reference-signature f64 resample_poly(2, 3)
+is compared bit for bit with the restated reference loop."""
+import numpy as np
+import pytest
+import scipy.signal as ss
+
+import oracle as O
+import scir_gb300 as S
+from conftest import normwise_err
+
+pytestmark = pytest.mark.gpu
+TOL_FP32 = 1e-5
+
+
+def _dev(a, cuda):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+
+
+@pytest.mark.parametrize("up,down,kh,n", [(3, 2, 11, 777), (1, 4, 9, 500), (5, 1, 22, 301),
+                                          (7, 3, 4, 1000), (160, 147, 3201, 5000), (2, 3, 31, 64),
+                                          (1, 1, 5, 100), (4, 1, 64, 2000), (300, 7, 50, 300)])
+def test_upfirdn_vs_oracle(cuda, up, down, kh, n):
+    rng = np.random.default_rng(up * 1000 + down + kh)
+    h = rng.standard_normal(kh).astype(np.float32)
+    x = rng.standard_normal((3, n)).astype(np.float32)
+    ref = O.upfirdn_f64(h.astype(np.float64), x.astype(np.float64), up, down)
+    y = S.upfirdn(_dev(h, cuda), _dev(x, cuda), up, down).cpu().numpy()
+    assert y.shape == ref.shape
+    assert normwise_err(y, ref) < TOL_FP32
+
+
+@pytest.mark.parametrize("up,down", [(160, 147), (3, 2), (2, 3), (1, 3), (5, 4), (4, 6)])
+def test_resample_default_design_vs_oracle(cuda, up, down):
+    rng = np.random.default_rng(up + down)
+    x = rng.standard_normal((4, 20000)).astype(np.float32)
+    h64 = S.resample_poly_default_taps(up, down, design=0)
+    h32 = h64.astype(np.float32)
+    ref = O.resample_poly_fast_f64(x.astype(np.float64), up, down, h32.astype(np.float64))
+    y = S.resample_poly_f32(_dev(x, cuda), up, down).cpu().numpy()
+    assert y.shape == ref.shape
+    assert normwise_err(y, ref) < TOL_FP32
+    # and against SciPy itself (FP64 design, FP64 data): the gap is the f32 rounding
+    assert normwise_err(y, ss.resample_poly(x.astype(np.float64), up, down, axis=1)) < 1e-5
+
+
+def test_resample_cfg2_full_size(cuda):
+    # 256 channels x 1,048,576 N(0,1) samples, 160/147, SciPy default 3,201-tap Kaiser(5)
+    import torch
+    g = torch.Generator(device=cuda).manual_seed(0)
+    x = torch.randn((256, 1048576), device=cuda, generator=g)
+    y = S.resample_poly_f32(x, 160, 147)
+    assert y.shape == (256, 1141308)
+    rows = [0, 255]
+    xs = x[rows].cpu().numpy().astype(np.float64)
+    h = S.resample_poly_default_taps(160, 147).astype(np.float32).astype(np.float64)
+    ref = O.resample_poly_fast_f64(xs, 160, 147, h)
+    assert normwise_err(y[rows].cpu().numpy(), ref) < TOL_FP32
+    del x, y
+    torch.cuda.empty_cache()
+
+
+def test_resample_explicit_taps_and_copy(cuda):
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((2, 1000)).astype(np.float32)
+    h = (rng.standard_normal(33) * 3).astype(np.float32)
+    ref = O.resample_poly_fast_f64(x.astype(np.float64), 3, 2, h.astype(np.float64))
+    y = S.resample_poly_f32(_dev(x, cuda), 3, 2, h=_dev(h, cuda)).cpu().numpy()
+    assert normwise_err(y, ref) < TOL_FP32
+    y = S.resample_poly_f32(_dev(x, cuda), 5, 5).cpu().numpy()
+    assert np.array_equal(y, x)
+
+
+def test_reference_resample_poly_2_3_bit_identical(cuda, golden_signal):
+    # crates/scir-signal/src/lib.rs:313-362 with its own design, f64
+    x = golden_signal["sosfilt_input"]
+    h = S.resample_poly_default_taps(2, 3, design=1)
+    ref = O.resample_poly_ref_f64(x, 2, 3, h)[0]
+    y = S.resample_poly(x, 2, 3)
+    assert np.array_equal(y, ref)
+    # crates/scir-signal/src/lib.rs:655-668 tolerance against SciPy's fixture
+    np.testing.assert_allclose(y, golden_signal["resample_poly_output"], atol=2e-2, rtol=1e-6)
+    rng = np.random.default_rng(4)
+    xb = rng.standard_normal((3, 5001))
+    assert np.array_equal(S.resample_poly(xb, 2, 3), O.resample_poly_ref_f64(xb, 2, 3, h))
+    with pytest.raises(S.GpuError):
+        S.resample_poly(xb, 160, 147)
+
+
+def test_resample_host_pipeline(cuda):
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((40, 300000)).astype(np.float32)
+    y = S.resample_poly_host(x, 160, 147)
+    h = S.resample_poly_default_taps(160, 147).astype(np.float32).astype(np.float64)
+    ref = O.resample_poly_fast_f64(x[::13].astype(np.float64), 160, 147, h)
+    assert normwise_err(y[::13], ref) < TOL_FP32

@@ -1,0 +1,122 @@
+"""Second-order-section filtering on the GPU vs the oracle.
+
+FP64_EXACT on f64 data is compared bit for bit with the restated reference
+DF2T loop.  FP32 data with FP64 state must be within 1e-5 normwise of the FP64
+oracle run on the same f32-rounded input.  The all-FP32 mode is reported, not
+bounded tightly (poles within 2e-4 of the unit circle)."""
+import numpy as np
+import pytest
+import scipy.signal as ss
+
+import oracle as O
+import scir_gb300 as S
+from conftest import normwise_err
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+SOS5 = ss.butter(8, [0.001, 0.002], btype="bandpass", output="sos")
+
+
+def _dev(a, cuda):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+
+
+@pytest.mark.parametrize("case", ["low_pass", "high_pass", "band_pass", "band_stop"])
+def test_strain_golden_bit_identical(cuda, golden_strain, case):
+    sos = golden_strain[f"sos_{case}"]
+    x = golden_strain["x"]
+    y = S.sosfilt(sos, x)
+    assert np.array_equal(y, O.sosfilt_f64(sos, x)[0])
+    np.testing.assert_allclose(y, golden_strain[f"y_{case}"], atol=1e-12, rtol=0)
+
+
+def test_signal_fixtures(cuda, golden_signal):
+    f = golden_signal
+    y = S.sosfilt(f["butter_sos"], f["sosfilt_input"])
+    np.testing.assert_allclose(y, f["sosfilt_output"], atol=1e-6, rtol=1e-6)
+    y = S.filtfilt(f["butter_sos"], f["sosfilt_input"])
+    np.testing.assert_allclose(y, f["filtfilt_output"], atol=1e-6, rtol=1e-6)
+    assert np.array_equal(y, O.filtfilt_ref_f64(f["butter_sos"], f["sosfilt_input"])[0])
+    for name in ["cheby", "bessel", "butter_hp", "cheby_hp", "bessel_hp", "notch"]:
+        y = S.sosfilt(f[f"{name}_sos"], f["sosfilt_input"])
+        np.testing.assert_allclose(y, f[f"{name}_output"], atol=1e-12, rtol=1e-12)
+
+
+@pytest.mark.parametrize("nsec", [1, 3, 8, 9, 16, 32])
+def test_exact_f64_any_section_count(cuda, nsec):
+    rng = np.random.default_rng(nsec)
+    sos = np.zeros((nsec, 6))
+    for i in range(nsec):  # stable random sections
+        r, th = rng.uniform(0.3, 0.95), rng.uniform(0, np.pi)
+        sos[i] = [rng.standard_normal(), rng.standard_normal(), rng.standard_normal(), 1.0,
+                  -2 * r * np.cos(th), r * r]
+    x = rng.standard_normal((70, 777))
+    y = S.sosfilt_f64(sos, _dev(x, cuda)).cpu().numpy()
+    assert np.array_equal(y, O.sosfilt_f64(sos, x))
+
+
+def test_cfg5_fp32_data_fp64_state(cuda):
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((96, 131072)).astype(np.float32)
+    ref = O.sosfilt_f64(SOS5, x.astype(np.float64))
+    y = S.sosfilt_f32(SOS5, _dev(x, cuda), precision=S.SosPrecision.FP64).cpu().numpy()
+    assert normwise_err(y, ref) < TOL
+    ye = S.sosfilt_f32(SOS5, _dev(x, cuda), precision=S.SosPrecision.FP64_EXACT).cpu().numpy()
+    assert normwise_err(ye, ref) < TOL
+    y32 = S.sosfilt_f32(SOS5, _dev(x, cuda), precision=S.SosPrecision.FP32).cpu().numpy()
+    e32 = normwise_err(y32, ref)
+    assert np.isfinite(y32).all() and e32 > TOL  # all-FP32 cannot hold 1e-5 on these poles
+    print(f"all-FP32 sosfilt normwise error {e32:.3e}")
+
+
+def test_state_chaining(cuda):
+    import torch
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((33, 5000))
+    xd = _dev(x, cuda)
+    y1, zf = S.sosfilt_f64(SOS5, xd[:, :2000].contiguous(), return_zf=True)
+    y2 = S.sosfilt_f64(SOS5, xd[:, 2000:].contiguous(), zi=zf)
+    full = torch.cat([y1, y2], 1).cpu().numpy()
+    assert np.array_equal(full, O.sosfilt_f64(SOS5, x))
+    zi = rng.standard_normal((33, 8, 2))
+    y, zf = S.sosfilt_f64(SOS5, xd, zi=_dev(zi, cuda), return_zf=True)
+    yr, zr = O.sosfilt_f64(SOS5, x, zi=zi, return_zf=True)
+    assert np.array_equal(y.cpu().numpy(), yr)
+    assert np.array_equal(zf.cpu().numpy(), zr)
+
+
+@pytest.mark.parametrize("padlen", [None, 0, 200])
+def test_sosfiltfilt_odd_vs_oracle(cuda, padlen):
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal((40, 20000))
+    ref = O.sosfiltfilt_f64(SOS5, x, padlen=padlen)
+    y = S.sosfiltfilt_f64(SOS5, _dev(x, cuda), padlen=padlen).cpu().numpy()
+    assert normwise_err(y, ref) < 1e-13
+    y32 = S.sosfiltfilt_f32(SOS5, _dev(x.astype(np.float32), cuda), padlen=padlen).cpu().numpy()
+    ref32 = O.sosfiltfilt_f64(SOS5, x.astype(np.float32).astype(np.float64), padlen=padlen)
+    assert normwise_err(y32, ref32) < TOL
+
+
+def test_sosfiltfilt_vs_scipy_and_in_place(cuda):
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((5, 9000))
+    xd = _dev(x, cuda)
+    y = S.sosfiltfilt_f64(SOS5, xd).cpu().numpy()
+    assert normwise_err(y, ss.sosfiltfilt(SOS5, x, axis=1)) < 1e-12
+    S.sosfiltfilt_f64(SOS5, xd, out=xd)  # y aliases x
+    assert normwise_err(xd.cpu().numpy(), y) == 0.0
+
+
+def test_unpadded_is_reference_filtfilt(cuda):
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal((7, 3000))
+    y = S.sosfiltfilt_f64(SOS5, _dev(x, cuda), padtype=S.PadType.NONE).cpu().numpy()
+    assert np.array_equal(y, O.filtfilt_ref_f64(SOS5, x))
+
+
+def test_short_signal_rejected(cuda):
+    x = _dev(np.ones((2, 51)), cuda)
+    with pytest.raises(S.GpuError) as ei:
+        S.sosfiltfilt_f64(SOS5, x)
+    assert ei.value.kind == "ShapeMismatch"
