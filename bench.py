@@ -153,10 +153,12 @@ class Resample(Workload):
     name = "resample_poly_160_147"
     B, N, UP, DOWN = 256, 1048576, 160, 147
 
-    def __init__(self, torch, dev, precision):
+    def __init__(self, torch, dev, precision, channels=None):
         import scir_gb300 as S
         self.S, self.torch, self.dev = S, torch, dev
         self.precision = precision
+        if channels:
+            self.B = channels
         g = torch.Generator(device=dev).manual_seed(0)
         self.x = torch.randn((self.B, self.N), device=dev, generator=g)
         self.n_out = S.resample_poly_out_len(self.N, self.UP, self.DOWN)
@@ -305,7 +307,7 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=dev)
     peaks = load_peaks()
     prec = S.Precision[args.precision]
-    W = WORKLOADS[args.workload](torch, dev, prec)
+    W = WORKLOADS[args.workload](torch, dev, prec, args.channels)
     stream = torch.cuda.current_stream(dev)
 
     def barrier():
@@ -399,7 +401,8 @@ def run_ours(args):
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded torch.randn on the device)",
-        "config": dict(W.config(), precision=prec.name, parallelism=f"replicas x{world}"),
+        "config": dict(W.config(), channels=W.B, precision=prec.name,
+                       parallelism=f"replicas x{world}"),
         "roofline": {"bound": W.bound, "achieved": achieved, "peak": peak, "unit": unit,
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": W.kernel, "kernel_ms": kern_ms,
@@ -425,6 +428,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="resample")
     ap.add_argument("--precision", default="AUTO")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--channels", type=int, default=None,
+                    help="override the channel count (profiling runs on a smaller case)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

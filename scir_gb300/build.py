@@ -45,6 +45,7 @@ def _compile(src: str, obj: str, verbose_ptxas: bool) -> None:
             cmd[1:1] = ["-Xptxas", "-v"]
     else:
         cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden",
+               "-ffp-contract=off",
                "-I", INCLUDE, "-I", CSRC, "-I", "/usr/local/cuda/include", "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

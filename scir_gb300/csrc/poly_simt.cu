@@ -6,130 +6,159 @@
 // 313-362), which multiplies every zero of the up-sampled signal through the
 // whole filter.
 //
-// Fast kernel (down <= up, ceil(kh/up) <= QM, up <= 256): outputs m and
-// m + up share their phase, and base advances by `down` per period.  A warp
-// takes one group of P consecutive outputs of the period (same phases in every
-// period) and its 32 lanes take 32 consecutive periods.  The group's P x
-// (QM+P-1) tap matrix -- each output's phase taps, shifted to the output's
-// offset inside a shared input window -- lives in registers, so each period
-// costs QM+P-1 shared loads and P*(QM+P-1) FMAs.  The CTA stages CT channels x
-// IT periods of input (zero outside [0, n)) and builds every group's tap
-// matrix in shared memory once.
+// Streaming kernel (down <= up, ceil(up/P) <= 32 groups for some P <= 5,
+// window fits the register budget): outputs m and m + up share their phase
+// and `base` advances by `down` per period.  A period is cut into G groups
+// of P consecutive outputs; lane l of every warp owns group l % G of period
+// offset l / G.  Each thread builds its P x JWA tap matrix once for the
+// whole (persistent) launch: each output's phase taps, shifted to the
+// output's place inside the lane's input window and pre-shifted by the
+// window's fixed misalignment so the window is read with 16-byte shared
+// loads.  Input windows (one channel, IP periods per work item) stream into a
+// 4-stage shared-memory ring by TMA (zero fill outside [0, n)), synchronised
+// by mbarriers with bounded waits.  Each warp stages its period's outputs in
+// shared memory and writes them back as contiguous 128-byte lines.
 //
-// Generic kernel: one thread per output, taps and input through the read-only
-// cache.  Used for down > up, very long phases or very large up.
+// Generic kernel: one thread per output, taps and input through the
+// read-only cache (down > up, long phases, misaligned rows).
 #include "common.cuh"
 #include "kernels.cuh"
+#include "sm100.cuh"
+
+#include <algorithm>
 
 namespace scir {
 namespace {
 
-constexpr int kP = 4;         // outputs per thread (consecutive in the period)
-constexpr int kCT = 2;        // channels per CTA
-constexpr int kIT = 64;       // periods per CTA
-constexpr int kThreads = 256; // 8 warps
-constexpr int kMaxUp = 256;
-
-__device__ __forceinline__ int padi(int j) { return j + (j >> 5); }
+constexpr int kNW = 8;          // warps per CTA
+constexpr int kThreads = kNW * 32;
+constexpr int kStages = 4;
+constexpr int kBox = 256;       // floats per TMA box
 
 struct PolyGeom {
-    int up, down, Q;
+    int up, down, Q, P, G, ppw;   // groups, periods per warp-iteration
     int64_t off;
-    int G;            // groups per period
-    int span;         // window positions one period of all groups touches
-    int WL;           // window length per channel for IT periods
-    int b00;          // base offset of rho = 0: off div up (mod the period)
+    int b00;                      // base of rho = 0 inside a period: off div up
+    int IP;                       // periods per work item
+    int nbox;                     // TMA boxes per stage
+    int stage_floats;
+    int64_t n_periods, items_per_row, n_items;
 };
 
-template <int QM>
-__global__ void __launch_bounds__(kThreads)
-poly_fast_kernel(const float* __restrict__ x, int64_t ld_x, int64_t batch, int64_t n,
-                 const float* __restrict__ h, int64_t kh, PolyGeom g,
-                 float* __restrict__ y, int64_t ld_y, int64_t n_out, int64_t n_periods,
-                 int64_t cta_per_row_group) {
-    constexpr int JW = QM + kP - 1;
-    constexpr int JWP = (JW + 3) / 4 * 4;
-    extern __shared__ __align__(16) float smem[];
-    float* s_T = smem;                          // [G][P][JWP]
-    float* s_x = smem + g.G * kP * JWP;         // [CT][padi(WL)]
-    const int WLP = padi(g.WL) + 1;
+template <int P, int JWA>
+__global__ void __launch_bounds__(kThreads, 1)
+poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restrict__ h,
+                   int64_t kh, const PolyGeom g, float* __restrict__ y, int64_t ld_y,
+                   int64_t n_out, unsigned* __restrict__ err) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    float* stages = reinterpret_cast<float*>(smem_raw);
+    float* ybuf = stages + kStages * g.stage_floats;
+    uint64_t* full = reinterpret_cast<uint64_t*>(ybuf + kNW * 32 * P);
 
-    const int64_t c0 = (blockIdx.x / cta_per_row_group) * kCT;
-    const int64_t i0 = (blockIdx.x % cta_per_row_group) * kIT;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int gl = lane % g.G, pl = lane / g.G;
+    const bool active = pl < g.ppw;
+    float* yb = ybuf + warp * 32 * P;
 
-    // tap matrices of every group
-    const int ntab = g.G * kP * JWP;
-    for (int e = tid; e < ntab; e += kThreads) {
-        const int jj = e % JWP, p = (e / JWP) % kP, gi = e / (JWP * kP);
-        const int rho = gi * kP + p;
-        float v = 0.0f;
-        if (rho < g.up && jj < JW) {
-            const int64_t t = (int64_t)rho * g.down + g.off;
-            const int64_t t0 = (int64_t)(gi * kP) * g.down + g.off;
-            const int ph = (int)(t % g.up);
-            const int d = (int)(t / g.up - t0 / g.up);
-            const int q = d + QM - 1 - jj;
+    // --- the thread's tap matrix, fixed for the whole launch
+    const int64_t t0 = (int64_t)(gl * P) * g.down + g.off;
+    const int rel0 = (int)(t0 / g.up) - g.b00;            // group window start in a period
+    const int64_t pos_first = (int64_t)g.b00 - (g.Q - 1); // window start of item 0 (i0 = 0)
+    const int shift = (int)(pos_first - (pos_first & ~(int64_t)3));
+    // window start inside the stage for this thread's first period (iteration 0)
+    const int L0 = (warp * g.ppw + pl) * g.down + rel0 + shift;
+    const int a = L0 & 3;
+    float T[P][JWA];
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+        const int rho = gl * P + p;
+        const int64_t t = (int64_t)rho * g.down + g.off;
+        const int ph = (int)(t % g.up);
+        const int d = (int)(t / g.up - t0 / g.up);
+#pragma unroll
+        for (int j = 0; j < JWA; ++j) {
+            const int q = d + g.Q - 1 + a - j;
             const int64_t hj = (int64_t)ph + (int64_t)q * g.up;
-            if (q >= 0 && q < g.Q && hj < kh) v = __ldg(h + hj);
+            T[p][j] = (rho < g.up && q >= 0 && q < g.Q && hj < kh) ? __ldg(h + hj) : 0.0f;
         }
-        s_T[e] = v;
     }
-    // input windows: positions pos_lo .. pos_lo + WL - 1 of each channel
-    const int64_t pos_lo = i0 * g.down + g.b00 - (QM - 1);
-    for (int c = 0; c < kCT; ++c) {
-        const int64_t row = c0 + c;
-        float* sx = s_x + c * WLP;
-        if (row < batch) {
-            const float* __restrict__ xr = x + row * ld_x;
-            for (int j = tid; j < g.WL; j += kThreads) {
-                const int64_t p = pos_lo + j;
-                sx[padi(j)] = (p >= 0 && p < n) ? __ldg(xr + p) : 0.0f;
-            }
-        }
+
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
+        fence_barrier_init();
+        prefetch_tmap(&xmap);
     }
     __syncthreads();
 
-    for (int gi = warp; gi < g.G; gi += kThreads / 32) {
-        float T[kP][JW];
-#pragma unroll
-        for (int p = 0; p < kP; ++p) {
-#pragma unroll
-            for (int j = 0; j < JWP; j += 4) {
-                const float4 t4 = *reinterpret_cast<const float4*>(s_T + (gi * kP + p) * JWP + j);
-                if (j < JW) T[p][j] = t4.x;
-                if (j + 1 < JW) T[p][j + 1] = t4.y;
-                if (j + 2 < JW) T[p][j + 2] = t4.z;
-                if (j + 3 < JW) T[p][j + 3] = t4.w;
-            }
+    auto issue = [&](int s, int64_t item) {
+        const int64_t row = item / g.items_per_row;
+        const int64_t i0 = (item % g.items_per_row) * g.IP;
+        const int64_t pos_lo = i0 * g.down + pos_first;
+        const int64_t pos_a = pos_lo & ~(int64_t)3;
+        float* dst = stages + s * g.stage_floats;
+        mbar_arrive_expect_tx(&full[s], (uint32_t)(g.nbox * kBox * sizeof(float)));
+        for (int b = 0; b < g.nbox; ++b)
+            tma_load_2d(dst + b * kBox, &xmap, &full[s], (int32_t)(pos_a + b * kBox), (int32_t)row);
+    };
+
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            const int64_t item = blockIdx.x + (int64_t)s * gridDim.x;
+            if (item < g.n_items) issue(s, item);
         }
-        const int rho0 = gi * kP;
-        const int64_t t0 = (int64_t)rho0 * g.down + g.off;
-        const int rel0 = (int)(t0 / g.up) - g.b00;  // window start of the group inside a period
-        for (int c = 0; c < kCT; ++c) {
-            const int64_t row = c0 + c;
-            if (row >= batch) break;
-            const float* sx = s_x + c * WLP;
-            float* __restrict__ yr = y + row * ld_y;
-            for (int ic = 0; ic < kIT; ic += 32) {
-                const int64_t i = i0 + ic + lane;
-                if (i >= n_periods) break;
-                const int rel = (ic + lane) * g.down + rel0;
-                float acc[kP];
+    }
+
+    const int iters = g.IP / g.ppw;  // warp-iterations per item
+    for (int64_t k = 0;; ++k) {
+        const int64_t item = blockIdx.x + k * gridDim.x;
+        if (item >= g.n_items) break;
+        const int s = (int)(k % kStages);
+        const uint32_t parity = (uint32_t)((k / kStages) & 1);
+        const bool ok = mbar_wait(&full[s], parity);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicOr(err, kErrMbarTimeout);
+            return;
+        }
+        const int64_t row = item / g.items_per_row;
+        const int64_t i0 = (item % g.items_per_row) * g.IP;
+        const float* win = stages + s * g.stage_floats;
+        float* __restrict__ yr = y + row * ld_y;
+        for (int it = warp; it < iters; it += kNW) {
+            const int po = it * g.ppw + pl;  // period offset inside the item
+            const int La = (po * g.down + rel0 + shift) & ~3;
+            float acc[P];
 #pragma unroll
-                for (int p = 0; p < kP; ++p) acc[p] = 0.0f;
+            for (int p = 0; p < P; ++p) acc[p] = 0.0f;
+            if (active) {
+                const float4* w4 = reinterpret_cast<const float4*>(win + La);
 #pragma unroll
-                for (int j = 0; j < JW; ++j) {
-                    const float w = sx[padi(rel + j)];
+                for (int j4 = 0; j4 < JWA / 4; ++j4) {
+                    const float4 w = w4[j4];
 #pragma unroll
-                    for (int p = 0; p < kP; ++p) acc[p] = fmaf(T[p][j], w, acc[p]);
+                    for (int p = 0; p < P; ++p) {
+                        acc[p] = fmaf(T[p][4 * j4 + 0], w.x, acc[p]);
+                        acc[p] = fmaf(T[p][4 * j4 + 1], w.y, acc[p]);
+                        acc[p] = fmaf(T[p][4 * j4 + 2], w.z, acc[p]);
+                        acc[p] = fmaf(T[p][4 * j4 + 3], w.w, acc[p]);
+                    }
                 }
-                const int64_t m0 = i * g.up + rho0;
 #pragma unroll
-                for (int p = 0; p < kP; ++p) {
-                    if (rho0 + p < g.up && m0 + p < n_out) yr[m0 + p] = acc[p];
-                }
+                for (int p = 0; p < P; ++p)
+                    if (gl * P + p < g.up) yb[pl * g.up + gl * P + p] = acc[p];
             }
+            __syncwarp();
+            const int64_t m0 = (i0 + (int64_t)it * g.ppw) * g.up;
+            const int cnt = g.ppw * g.up;
+            for (int e = lane; e < cnt; e += 32) {
+                const int64_t m = m0 + e;
+                if (m < n_out) yr[m] = yb[e];
+            }
+            __syncwarp();
+        }
+        __syncthreads();  // stage s fully consumed
+        if (tid == 0) {
+            const int64_t next = item + (int64_t)kStages * gridDim.x;
+            if (next < g.n_items) issue(s, next);
         }
     }
 }
@@ -153,62 +182,93 @@ poly_generic_kernel(const float* __restrict__ x, int64_t ld_x, int64_t n,
     y[row * ld_y + m] = acc;
 }
 
-template <int QM>
-int launch_fast(const PolyArgs& a, int Q, cudaStream_t st) {
-    constexpr int JW = QM + kP - 1;
-    constexpr int JWP = (JW + 3) / 4 * 4;
+template <int P, int JWA>
+int launch_stream(const PolyArgs& a, const PolyGeom& g0, cudaStream_t st) {
+    const DeviceInfo* info = nullptr;
+    int rc = current_device(&info);
+    if (rc) return rc;
+    PolyGeom g = g0;
+    const size_t smem = sizeof(float) * ((size_t)kStages * g.stage_floats + kNW * 32 * P) +
+                        kStages * sizeof(uint64_t);
+    if ((int)smem > info->max_smem_optin)
+        return set_error(SCIR_ERR_UNSUPPORTED, "polyphase stage needs %zu bytes", smem);
+    CUtensorMap map;
+    rc = make_tmap_2d(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, a.x, (uint64_t)a.n, (uint64_t)a.batch,
+                      (uint64_t)a.ld_x * sizeof(float), kBox, 1, CU_TENSOR_MAP_SWIZZLE_NONE);
+    if (rc) return rc;
+    unsigned* err = device_error_word();
+    if (!err) return set_error(SCIR_ERR_CUDA, "device error word unavailable");
+    auto kern = poly_stream_kernel<P, JWA>;
+    SCIR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t grid = std::min<int64_t>(g.n_items, (int64_t)info->sm_count);
+    kern<<<(unsigned)grid, kThreads, smem, st>>>(map, a.h, a.kh, g, a.y, a.ld_y, a.n_out, err);
+    SCIR_LAUNCH_CHECK("poly_stream_kernel");
+    return SCIR_OK;
+}
+
+// Window lengths with a compiled kernel (multiples of 4).
+int jwa_bucket(int jwa) { return jwa <= 12 ? 12 : jwa <= 20 ? 20 : jwa <= 28 ? 28 : 36; }
+
+template <int P>
+int dispatch_jwa(const PolyArgs& a, const PolyGeom& g, int jwa_b, cudaStream_t st) {
+    switch (jwa_b) {
+    case 12: return launch_stream<P, 12>(a, g, st);
+    case 20: return launch_stream<P, 20>(a, g, st);
+    case 28: return launch_stream<P, 28>(a, g, st);
+    default: return launch_stream<P, 36>(a, g, st);
+    }
+}
+
+int try_stream(const PolyArgs& a, cudaStream_t st) {
+    if (a.down > a.up) return SCIR_ERR_UNSUPPORTED;
+    if ((reinterpret_cast<uintptr_t>(a.x) & 15) || (a.ld_x & 3)) return SCIR_ERR_UNSUPPORTED;
+    if (a.n >= (1LL << 31) - 4096 || a.batch >= (1LL << 31)) return SCIR_ERR_UNSUPPORTED;
+    const int64_t Q = ceil_div(a.kh, a.up);
+    int P = (int)ceil_div(a.up, 32);
+    if (P < 1) P = 1;
+    if (P > 5) return SCIR_ERR_UNSUPPORTED;
+    const int JW = (int)Q + P - 1;
+    const int jwa = (JW + 3 + 3) / 4 * 4;
+    if (jwa > 36) return SCIR_ERR_UNSUPPORTED;
+    const int jwa_b = jwa_bucket(jwa);
     PolyGeom g;
     g.up = a.up;
     g.down = a.down;
-    g.Q = Q;
+    g.Q = (int)Q;
+    g.P = P;
+    g.G = (int)ceil_div(a.up, P);
+    g.ppw = 32 / g.G;
     g.off = a.off;
-    g.G = (a.up + kP - 1) / kP;
-    g.b00 = (int)((a.off) / a.up);
+    g.b00 = (int)(a.off / a.up);
+    g.IP = 32 * g.ppw;
     int maxrel = 0;
     for (int gi = 0; gi < g.G; ++gi) {
-        const int64_t t0 = (int64_t)(gi * kP) * a.down + a.off;
-        maxrel = max(maxrel, (int)(t0 / a.up) - g.b00);
+        const int64_t t0 = (int64_t)(gi * P) * a.down + a.off;
+        maxrel = std::max(maxrel, (int)(t0 / a.up) - g.b00);
     }
-    g.span = maxrel + JW;
-    g.WL = (kIT - 1) * a.down + g.span;
-    const int WLP = g.WL + g.WL / 32 + 1;
-    const size_t smem = sizeof(float) * ((size_t)g.G * kP * JWP + (size_t)kCT * WLP);
-    const int64_t n_periods = ceil_div(a.n_out, a.up);
-    const int64_t per_row_group = ceil_div(n_periods, kIT);
-    const int64_t grid = per_row_group * ceil_div(a.batch, kCT);
-    SCIR_REQUIRE(grid <= 0x7fffffffLL, SCIR_ERR_UNSUPPORTED, "polyphase grid too large");
-    const scir::DeviceInfo* info = nullptr;
-    int rc = current_device(&info);
-    if (rc) return rc;
-    SCIR_REQUIRE((int)smem <= info->max_smem_optin, SCIR_ERR_UNSUPPORTED,
-                 "polyphase tile needs %zu bytes of shared memory", smem);
-    auto kern = poly_fast_kernel<QM>;
-    SCIR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<(unsigned)grid, kThreads, smem, st>>>(a.x, a.ld_x, a.batch, a.n, a.h, a.kh, g, a.y,
-                                                 a.ld_y, a.n_out, n_periods, per_row_group);
-    SCIR_LAUNCH_CHECK("poly_fast_kernel");
-    return SCIR_OK;
+    const int64_t need = (int64_t)(g.IP - 1) * a.down + maxrel + 3 + jwa_b + 4;
+    if (need > 48 * 1024) return SCIR_ERR_UNSUPPORTED;
+    g.nbox = (int)ceil_div(need, kBox);
+    g.stage_floats = g.nbox * kBox;
+    g.n_periods = ceil_div(a.n_out, a.up);
+    g.items_per_row = ceil_div(g.n_periods, g.IP);
+    g.n_items = g.items_per_row * a.batch;
+    switch (P) {
+    case 1: return dispatch_jwa<1>(a, g, jwa_b, st);
+    case 2: return dispatch_jwa<2>(a, g, jwa_b, st);
+    case 3: return dispatch_jwa<3>(a, g, jwa_b, st);
+    case 4: return dispatch_jwa<4>(a, g, jwa_b, st);
+    default: return dispatch_jwa<5>(a, g, jwa_b, st);
+    }
 }
 
 }  // namespace
 
 int launch_poly_simt(const PolyArgs& a, cudaStream_t st) {
     if (a.batch == 0 || a.n_out == 0) return SCIR_OK;
-    const int64_t Q = ceil_div(a.kh, a.up);
-    if (a.down <= a.up && a.up <= kMaxUp && Q <= 32 && a.down * (int64_t)kIT < (1 << 20)) {
-        int rc = SCIR_ERR_UNSUPPORTED;
-        if (Q <= 4) rc = launch_fast<4>(a, (int)Q, st);
-        else if (Q <= 8) rc = launch_fast<8>(a, (int)Q, st);
-        else if (Q <= 12) rc = launch_fast<12>(a, (int)Q, st);
-        else if (Q <= 16) rc = launch_fast<16>(a, (int)Q, st);
-        else if (Q <= 20) rc = launch_fast<20>(a, (int)Q, st);
-        else if (Q <= 22) rc = launch_fast<22>(a, (int)Q, st);
-        else if (Q <= 24) rc = launch_fast<24>(a, (int)Q, st);
-        else if (Q <= 28) rc = launch_fast<28>(a, (int)Q, st);
-        else rc = launch_fast<32>(a, (int)Q, st);
-        if (rc != SCIR_ERR_UNSUPPORTED) return rc;
-        clear_error();
-    }
+    int rc = try_stream(a, st);
+    if (rc != SCIR_ERR_UNSUPPORTED) return rc;
+    clear_error();
     const int64_t bpr = ceil_div(a.n_out, 256);
     const int64_t grid = bpr * a.batch;
     SCIR_REQUIRE(grid <= 0x7fffffffLL, SCIR_ERR_UNSUPPORTED, "polyphase grid too large");

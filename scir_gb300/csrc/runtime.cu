@@ -7,6 +7,9 @@
 // per-device facts are cached once, and errors are status codes plus a
 // thread-local message.
 #include "common.cuh"
+#include "sm100.cuh"
+
+#include <cudaTypedefs.h>
 
 #include <cstdarg>
 #include <cstdio>
@@ -109,6 +112,74 @@ int scratch_alloc(void** p, size_t bytes, cudaStream_t stream) {
 
 void scratch_free(void* p, cudaStream_t stream) {
     if (p) cudaFreeAsync(p, stream);
+}
+
+int make_tmap_2d(CUtensorMap* map, CUtensorMapDataType dtype, const void* base, uint64_t dim0,
+                 uint64_t dim1, uint64_t stride1_bytes, uint32_t box0, uint32_t box1,
+                 CUtensorMapSwizzle swizzle) {
+    static std::mutex mu;
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!encode) {
+            void* fn = nullptr;
+            cudaDriverEntryPointQueryResult q;
+            SCIR_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                           cudaEnableDefault, &q));
+            if (!fn || q != cudaDriverEntryPointSuccess)
+                return set_error(SCIR_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        }
+    }
+    if ((reinterpret_cast<uintptr_t>(base) & 15) || (stride1_bytes & 15))
+        return set_error(SCIR_ERR_ALIGN, "TMA needs a 16-byte aligned base and row stride");
+    cuuint64_t dims[2] = {dim0, dim1};
+    cuuint64_t strides[1] = {stride1_bytes};
+    cuuint32_t box[2] = {box0, box1};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode(map, dtype, 2, const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return set_error(SCIR_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return SCIR_OK;
+}
+
+namespace {
+std::mutex g_err_mutex;
+unsigned* g_err_word[kMaxDevices] = {};
+}  // namespace
+
+unsigned* device_error_word() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(g_err_mutex);
+    if (!g_err_word[dev]) {
+        unsigned* p = nullptr;
+        if (cudaMalloc(&p, sizeof(unsigned)) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        unsigned zero = 0;
+        if (upload_sync(p, &zero, sizeof(zero)) != SCIR_OK) return nullptr;
+        g_err_word[dev] = p;
+    }
+    return g_err_word[dev];
+}
+
+int device_error_take(unsigned* code) {
+    *code = 0;
+    unsigned* w = device_error_word();
+    if (!w) return set_error(SCIR_ERR_CUDA, "no device error word");
+    SCIR_CUDA_TRY(cudaMemcpy(code, w, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (*code) {
+        unsigned zero = 0;
+        return upload_sync(w, &zero, sizeof(zero));
+    }
+    return SCIR_OK;
 }
 
 }  // namespace scir
