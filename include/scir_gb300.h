@@ -128,6 +128,11 @@ SCIR_API int scir_last_error(char* buf, size_t len);
  * (crates/scir-gpu/src/lib.rs:596-616). */
 SCIR_API int scir_init(int device);
 SCIR_API int scir_device_count(int* count);
+/* Reads and clears the current device's error word: non-zero when a kernel's
+ * bounded device-side wait gave up (1) or a kernel rejected its geometry (2)
+ * since the last call.  Synchronises with the device.  The reference has no
+ * device-side failure reporting (its CUDA path cannot run at all). */
+SCIR_API int scir_device_errors(unsigned* code);
 
 /* ----------------------------------------------------------------------- */
 /* Batched FIR (device pointers, stream-ordered)                           */

@@ -29,7 +29,7 @@ __all__ = [
     "resample_poly", "resample_poly_host", "fir_batched", "fir_out_len", "upfirdn",
     "upfirdn_out_len", "resample_poly_f32", "resample_poly_out_len", "resample_poly_default_taps",
     "sosfilt_f32", "sosfilt_f64", "sosfiltfilt_f32", "sosfiltfilt_f64", "sosfilt_zi",
-    "sosfiltfilt_default_padlen", "RaggedPlan", "load",
+    "sosfiltfilt_default_padlen", "RaggedPlan", "load", "device_errors",
 ]
 
 OK, ERR_INVALID_ARG, ERR_SHAPE, ERR_ALIGN, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED, \
@@ -184,6 +184,14 @@ def resample_poly_host(x, up: int, down: int, h=None,
                                               0 if hh is None else hh.size, int(precision),
                                               _ptr(y)))
     return y
+
+
+def device_errors() -> int:
+    """Reads and clears the device error word (non-zero: a kernel's bounded
+    wait gave up).  Synchronises the device."""
+    code = ctypes.c_uint(0)
+    _check(load().scir_device_errors(ctypes.byref(code)))
+    return int(code.value)
 
 
 def fir_out_len(n: int, k: int, mode: FirMode) -> int:

@@ -15,9 +15,14 @@
 // output's place inside the lane's input window and pre-shifted by the
 // window's fixed misalignment so the window is read with 16-byte shared
 // loads.  Input windows (one channel, IP periods per work item) stream into a
-// 4-stage shared-memory ring by TMA (zero fill outside [0, n)), synchronised
-// by mbarriers with bounded waits.  Each warp stages its period's outputs in
-// shared memory and writes them back as contiguous 128-byte lines.
+// 4-stage shared-memory ring by TMA (zero fill outside [0, n)).  No warp ever
+// waits for another: each warp waits only for its stage's data (mbarrier,
+// bounded wait), and the last warp to finish with a stage (a shared-memory
+// counter) issues that stage's refill for the item four steps ahead.
+// Which lane takes which group is a per-warp permutation chosen on the host
+// to spread the lanes' 16-byte window reads over the shared-memory banks.
+// Each warp stages its period's outputs in shared memory and writes them
+// back as contiguous 128-byte lines.
 //
 // Generic kernel: one thread per output, taps and input through the
 // read-only cache (down > up, long phases, misaligned rows).
@@ -43,28 +48,58 @@ struct PolyGeom {
     int nbox;                     // TMA boxes per stage
     int stage_floats;
     int64_t n_periods, items_per_row, n_items;
+    uint8_t unit[kNW][32];        // work unit (pl * G + gl) of each lane; 255 = idle
 };
 
 template <int P, int JWA>
 __global__ void __launch_bounds__(kThreads, 1)
 poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restrict__ h,
-                   int64_t kh, const PolyGeom g, float* __restrict__ y, int64_t ld_y,
-                   int64_t n_out, unsigned* __restrict__ err) {
+                   int64_t kh, const __grid_constant__ PolyGeom g, float* __restrict__ y,
+                   int64_t ld_y, int64_t n_out, unsigned* __restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     float* stages = reinterpret_cast<float*>(smem_raw);
     float* ybuf = stages + kStages * g.stage_floats;
     uint64_t* full = reinterpret_cast<uint64_t*>(ybuf + kNW * 32 * P);
+    int* done = reinterpret_cast<int*>(full + kStages);  // warps finished with each stage
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int gl = lane % g.G, pl = lane / g.G;
-    const bool active = pl < g.ppw;
+    const int64_t pos_first = (int64_t)g.b00 - (g.Q - 1);  // window start of item 0 (i0 = 0)
+    const int shift = (int)(pos_first - (pos_first & ~(int64_t)3));
+
+    auto issue = [&](int s, int64_t item) {
+        const int64_t row = item / g.items_per_row;
+        const int64_t i0 = (item % g.items_per_row) * g.IP;
+        const int64_t pos_a = (i0 * g.down + pos_first) & ~(int64_t)3;
+        float* dst = stages + s * g.stage_floats;
+        mbar_arrive_expect_tx(&full[s], (uint32_t)(g.nbox * kBox * sizeof(float)));
+        for (int b = 0; b < g.nbox; ++b)
+            tma_load_2d(dst + b * kBox, &xmap, &full[s], (int32_t)(pos_a + b * kBox), (int32_t)row);
+    };
+
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            done[s] = 0;
+        }
+        fence_barrier_init();
+        prefetch_tmap(&xmap);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            const int64_t item = blockIdx.x + (int64_t)s * gridDim.x;
+            if (item < g.n_items) issue(s, item);
+        }
+    }
+
+    const int unit = g.unit[warp][lane];
+    const bool active = unit < g.G * g.ppw;
+    const int gl = active ? unit % g.G : 0, pl = active ? unit / g.G : 0;
     float* yb = ybuf + warp * 32 * P;
 
     // --- the thread's tap matrix, fixed for the whole launch
     const int64_t t0 = (int64_t)(gl * P) * g.down + g.off;
-    const int rel0 = (int)(t0 / g.up) - g.b00;            // group window start in a period
-    const int64_t pos_first = (int64_t)g.b00 - (g.Q - 1); // window start of item 0 (i0 = 0)
-    const int shift = (int)(pos_first - (pos_first & ~(int64_t)3));
+    const int rel0 = (int)(t0 / g.up) - g.b00;  // group window start in a period
     // window start inside the stage for this thread's first period (iteration 0)
     const int L0 = (warp * g.ppw + pl) * g.down + rel0 + shift;
     const int a = L0 & 3;
@@ -79,32 +114,7 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
         for (int j = 0; j < JWA; ++j) {
             const int q = d + g.Q - 1 + a - j;
             const int64_t hj = (int64_t)ph + (int64_t)q * g.up;
-            T[p][j] = (rho < g.up && q >= 0 && q < g.Q && hj < kh) ? __ldg(h + hj) : 0.0f;
-        }
-    }
-
-    if (tid == 0) {
-        for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
-        fence_barrier_init();
-        prefetch_tmap(&xmap);
-    }
-    __syncthreads();
-
-    auto issue = [&](int s, int64_t item) {
-        const int64_t row = item / g.items_per_row;
-        const int64_t i0 = (item % g.items_per_row) * g.IP;
-        const int64_t pos_lo = i0 * g.down + pos_first;
-        const int64_t pos_a = pos_lo & ~(int64_t)3;
-        float* dst = stages + s * g.stage_floats;
-        mbar_arrive_expect_tx(&full[s], (uint32_t)(g.nbox * kBox * sizeof(float)));
-        for (int b = 0; b < g.nbox; ++b)
-            tma_load_2d(dst + b * kBox, &xmap, &full[s], (int32_t)(pos_a + b * kBox), (int32_t)row);
-    };
-
-    if (tid == 0) {
-        for (int s = 0; s < kStages; ++s) {
-            const int64_t item = blockIdx.x + (int64_t)s * gridDim.x;
-            if (item < g.n_items) issue(s, item);
+            T[p][j] = (active && rho < g.up && q >= 0 && q < g.Q && hj < kh) ? __ldg(h + hj) : 0.0f;
         }
     }
 
@@ -114,10 +124,9 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
         if (item >= g.n_items) break;
         const int s = (int)(k % kStages);
         const uint32_t parity = (uint32_t)((k / kStages) & 1);
-        const bool ok = mbar_wait(&full[s], parity);
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) atomicOr(err, kErrMbarTimeout);
-            return;
+        if (!mbar_wait(&full[s], parity)) {
+            if (lane == 0) atomicOr(err, kErrMbarTimeout);
+            break;
         }
         const int64_t row = item / g.items_per_row;
         const int64_t i0 = (item % g.items_per_row) * g.IP;
@@ -155,10 +164,16 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
             }
             __syncwarp();
         }
-        __syncthreads();  // stage s fully consumed
-        if (tid == 0) {
-            const int64_t next = item + (int64_t)kStages * gridDim.x;
-            if (next < g.n_items) issue(s, next);
+        // the last warp done with stage s refills it (the fences order every
+        // warp's reads of the stage before the refill's writes)
+        if (lane == 0) {
+            __threadfence_block();
+            if (atomicAdd(&done[s], 1) == kNW - 1) {
+                __threadfence_block();
+                done[s] = 0;
+                const int64_t next = item + (int64_t)kStages * gridDim.x;
+                if (next < g.n_items) issue(s, next);
+            }
         }
     }
 }
@@ -189,7 +204,7 @@ int launch_stream(const PolyArgs& a, const PolyGeom& g0, cudaStream_t st) {
     if (rc) return rc;
     PolyGeom g = g0;
     const size_t smem = sizeof(float) * ((size_t)kStages * g.stage_floats + kNW * 32 * P) +
-                        kStages * sizeof(uint64_t);
+                        kStages * (sizeof(uint64_t) + sizeof(int));
     if ((int)smem > info->max_smem_optin)
         return set_error(SCIR_ERR_UNSUPPORTED, "polyphase stage needs %zu bytes", smem);
     CUtensorMap map;
@@ -216,6 +231,68 @@ int dispatch_jwa(const PolyArgs& a, const PolyGeom& g, int jwa_b, cudaStream_t s
     case 20: return launch_stream<P, 20>(a, g, st);
     case 28: return launch_stream<P, 28>(a, g, st);
     default: return launch_stream<P, 36>(a, g, st);
+    }
+}
+
+// 16-byte shared wavefronts a warp needs for one window load: lanes are served
+// in quarters of 8; two lanes conflict when their 16-byte chunks differ but
+// map to the same 4-bank quad (chunk mod 8).
+int quarter_wavefronts(const int* chunk) {
+    int total = 0;
+    for (int q = 0; q < 4; ++q) {
+        int worst = 1;
+        for (int r = 0; r < 8; ++r) {
+            int seen[8], ns = 0;
+            for (int l = 8 * q; l < 8 * q + 8; ++l) {
+                if (chunk[l] < 0 || (chunk[l] & 7) != r) continue;
+                bool dup = false;
+                for (int i = 0; i < ns; ++i) dup |= seen[i] == chunk[l];
+                if (!dup) seen[ns++] = chunk[l];
+            }
+            worst = std::max(worst, ns);
+        }
+        total += worst;
+    }
+    return total;
+}
+
+// Chooses, per warp, which lane takes which (group, period) unit so that the
+// lanes' window reads hit distinct bank quads as far as possible (a short
+// deterministic local search over lane swaps).
+void assign_lanes(PolyGeom& g, int /*maxrel*/) {
+    const int64_t pos_first = (int64_t)g.b00 - (g.Q - 1);
+    const int shift = (int)(pos_first - (pos_first & ~(int64_t)3));
+    const int nunits = g.G * g.ppw;
+    uint32_t rng = 12345u;
+    for (int w = 0; w < kNW; ++w) {
+        int unit[32], chunk[32];
+        for (int l = 0; l < 32; ++l) unit[l] = l < nunits ? l : 255;
+        auto chunk_of = [&](int u) {
+            if (u == 255) return -1;
+            const int gl = u % g.G, pl = u / g.G;
+            const int64_t t0 = (int64_t)(gl * g.P) * g.down + g.off;
+            const int rel0 = (int)(t0 / g.up) - g.b00;
+            return (((w * g.ppw + pl) * g.down + rel0 + shift) & ~3) / 4;
+        };
+        for (int l = 0; l < 32; ++l) chunk[l] = chunk_of(unit[l]);
+        int cur = quarter_wavefronts(chunk);
+        for (int step = 0; step < 3000 && cur > 4; ++step) {
+            rng = rng * 1664525u + 1013904223u;
+            const int i = (int)((rng >> 8) & 31);
+            rng = rng * 1664525u + 1013904223u;
+            const int j = (int)((rng >> 8) & 31);
+            if (i / 8 == j / 8) continue;
+            std::swap(unit[i], unit[j]);
+            std::swap(chunk[i], chunk[j]);
+            const int v = quarter_wavefronts(chunk);
+            if (v <= cur) {
+                cur = v;
+            } else {
+                std::swap(unit[i], unit[j]);
+                std::swap(chunk[i], chunk[j]);
+            }
+        }
+        for (int l = 0; l < 32; ++l) g.unit[w][l] = (uint8_t)unit[l];
     }
 }
 
@@ -253,6 +330,7 @@ int try_stream(const PolyArgs& a, cudaStream_t st) {
     g.n_periods = ceil_div(a.n_out, a.up);
     g.items_per_row = ceil_div(g.n_periods, g.IP);
     g.n_items = g.items_per_row * a.batch;
+    assign_lanes(g, maxrel);
     switch (P) {
     case 1: return dispatch_jwa<1>(a, g, jwa_b, st);
     case 2: return dispatch_jwa<2>(a, g, jwa_b, st);

@@ -114,9 +114,9 @@ void scratch_free(void* p, cudaStream_t stream) {
     if (p) cudaFreeAsync(p, stream);
 }
 
-int make_tmap_2d(CUtensorMap* map, CUtensorMapDataType dtype, const void* base, uint64_t dim0,
-                 uint64_t dim1, uint64_t stride1_bytes, uint32_t box0, uint32_t box1,
-                 CUtensorMapSwizzle swizzle) {
+static int tmap_encode(CUtensorMap* map, CUtensorMapDataType dtype, int rank, const void* base,
+                       const uint64_t* dims, const uint64_t* strides_bytes, const uint32_t* box,
+                       CUtensorMapSwizzle swizzle) {
     static std::mutex mu;
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     {
@@ -131,18 +131,40 @@ int make_tmap_2d(CUtensorMap* map, CUtensorMapDataType dtype, const void* base, 
             encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
         }
     }
-    if ((reinterpret_cast<uintptr_t>(base) & 15) || (stride1_bytes & 15))
-        return set_error(SCIR_ERR_ALIGN, "TMA needs a 16-byte aligned base and row stride");
-    cuuint64_t dims[2] = {dim0, dim1};
-    cuuint64_t strides[1] = {stride1_bytes};
-    cuuint32_t box[2] = {box0, box1};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = encode(map, dtype, 2, const_cast<void*>(base), dims, strides, box, estr,
+    if (reinterpret_cast<uintptr_t>(base) & 15)
+        return set_error(SCIR_ERR_ALIGN, "TMA needs a 16-byte aligned base address");
+    cuuint64_t d[3], st[2];
+    cuuint32_t b[3], es[3] = {1, 1, 1};
+    for (int i = 0; i < rank; ++i) {
+        d[i] = dims[i];
+        b[i] = box[i];
+    }
+    for (int i = 0; i + 1 < rank; ++i) {
+        if (strides_bytes[i] & 15) return set_error(SCIR_ERR_ALIGN, "TMA row stride must be a multiple of 16 bytes");
+        st[i] = strides_bytes[i];
+    }
+    CUresult r = encode(map, dtype, (cuuint32_t)rank, const_cast<void*>(base), d, st, b, es,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
         return set_error(SCIR_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return SCIR_OK;
+}
+
+int make_tmap_2d(CUtensorMap* map, CUtensorMapDataType dtype, const void* base, uint64_t dim0,
+                 uint64_t dim1, uint64_t stride1_bytes, uint32_t box0, uint32_t box1,
+                 CUtensorMapSwizzle swizzle) {
+    const uint64_t dims[2] = {dim0, dim1}, strides[1] = {stride1_bytes};
+    const uint32_t box[2] = {box0, box1};
+    return tmap_encode(map, dtype, 2, base, dims, strides, box, swizzle);
+}
+
+int make_tmap_3d(CUtensorMap* map, CUtensorMapDataType dtype, const void* base, uint64_t dim0,
+                 uint64_t dim1, uint64_t dim2, uint64_t stride1_bytes, uint64_t stride2_bytes,
+                 uint32_t box0, uint32_t box1, uint32_t box2, CUtensorMapSwizzle swizzle) {
+    const uint64_t dims[3] = {dim0, dim1, dim2}, strides[2] = {stride1_bytes, stride2_bytes};
+    const uint32_t box[3] = {box0, box1, box2};
+    return tmap_encode(map, dtype, 3, base, dims, strides, box, swizzle);
 }
 
 namespace {
@@ -220,6 +242,12 @@ SCIR_API int scir_device_count(int* count) {
         return scir::set_error(SCIR_ERR_NO_DEVICE, "cudaGetDeviceCount: %s", cudaGetErrorString(e));
     }
     return SCIR_OK;
+}
+
+SCIR_API int scir_device_errors(unsigned* code) {
+    if (!code) return scir::set_error(SCIR_ERR_INVALID_ARG, "code is NULL");
+    SCIR_CUDA_TRY(cudaDeviceSynchronize());
+    return scir::device_error_take(code);
 }
 
 SCIR_API int scir_init(int device) {

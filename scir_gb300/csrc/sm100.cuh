@@ -56,16 +56,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Waits for the phase with the given parity to complete.  Gives up after
-// `limit` polls (each try_wait itself suspends for a while); returns false on
-// timeout so the caller can record the error and leave.
+// Waits for the phase with the given parity to complete.  try_wait itself
+// suspends the thread in hardware for a while, so the loop does not sleep;
+// it gives up once `limit_cycles` SM clock cycles have passed (about two
+// seconds by default) and returns false so the caller can record the error
+// and leave.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
-                                          uint32_t limit = (1u << 26)) {
-    for (uint32_t i = 0; i < limit; ++i) {
+                                          long long limit_cycles = 4000000000LL) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    for (uint32_t i = 1;; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (i > 64) __nanosleep(32);
+        if ((i & 63) == 0 && clock64() - t0 > limit_cycles) return false;
     }
-    return false;
 }
 
 // ------------------------------------------------------------------ TMA
@@ -79,6 +82,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
         "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
         " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
         "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int32_t c0, int32_t c1, int32_t c2) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
         : "memory");
 }
 
@@ -186,6 +198,10 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
 int make_tmap_2d(CUtensorMap* map, CUtensorMapDataType dtype, const void* base, uint64_t dim0,
                  uint64_t dim1, uint64_t stride1_bytes, uint32_t box0, uint32_t box1,
                  CUtensorMapSwizzle swizzle);
+// Rank-3 variant: dims {dim0, dim1, dim2}, strides of dims 1 and 2 in bytes.
+int make_tmap_3d(CUtensorMap* map, CUtensorMapDataType dtype, const void* base, uint64_t dim0,
+                 uint64_t dim1, uint64_t dim2, uint64_t stride1_bytes, uint64_t stride2_bytes,
+                 uint32_t box0, uint32_t box1, uint32_t box2, CUtensorMapSwizzle swizzle);
 
 // Reads and clears the device error word of the current device.
 int device_error_take(unsigned* code);

@@ -37,7 +37,10 @@ def cuda():
     assert torch.cuda.is_available(), "GPU test run without a CUDA device"
     import scir_gb300
     scir_gb300.load()
-    return torch.device("cuda:0")
+    assert scir_gb300.device_errors() == 0
+    yield torch.device("cuda:0")
+    # no kernel of the session may have given up a bounded device-side wait
+    assert scir_gb300.device_errors() == 0
 
 
 def normwise_err(y, ref):

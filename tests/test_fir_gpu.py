@@ -126,3 +126,62 @@ def test_host_pipeline_many_chunks(cuda):
     taps = rng.standard_normal(15).astype(np.float32)
     y = S.fir_batched_host(x, taps, S.FirMode.REF_CORR, S.Precision.REF_EXACT)
     assert np.array_equal(y[::37], O.fir1d_batched_f32(x[::37], taps))
+
+
+# ---------------------------------------------------------------- tensor cores
+# BF16X6 (three bf16 terms, six products) must meet the FP32 bound of 1e-5;
+# BF16X3 (hi+lo, three products) carries ~16 significant bits per product and
+# is held to a stated bound of 3e-5 normwise (about 7e-6 on the long-tap
+# band-pass workload).
+TOL_BF16X3 = 3e-5
+
+
+@pytest.mark.parametrize("prec,tol", [(S.Precision.BF16X6, TOL_FP32), (S.Precision.BF16X3, TOL_BF16X3)])
+@pytest.mark.parametrize("mode", list(S.FirMode))
+@pytest.mark.parametrize("b,n,k", [(3, 1000, 63), (130, 3000, 700), (2, 40000, 4095), (1, 300, 1)])
+def test_tensor_core_vs_fp64(cuda, prec, tol, mode, b, n, k):
+    if mode == S.FirMode.VALID and n < k:
+        pytest.skip("VALID needs n >= k")
+    rng = np.random.default_rng(b + n + k + int(mode))
+    x = rng.uniform(-1, 1, (b, n)).astype(np.float32)
+    taps = (rng.standard_normal(k) / np.sqrt(k)).astype(np.float32)
+    ref = O.fir_mode_f64(x.astype(np.float64), taps.astype(np.float64), int(mode))
+    y = S.fir_batched(_dev(x, cuda), _dev(taps, cuda), mode, prec).cpu().numpy()
+    assert y.shape == ref.shape
+    err = normwise_err(y, ref)
+    assert err < tol, err
+
+
+def test_tensor_core_cfg3_bandpass(cuda):
+    # the long-tap configuration's filter and signal family, 130 channels
+    rng = np.random.default_rng(0)
+    n = 32768
+    t = np.arange(n)
+    x = np.zeros((130, n))
+    for c in range(130):
+        f = rng.uniform(0, 0.5, 32)
+        ph = rng.uniform(0, 2 * np.pi, 32)
+        x[c] = np.sum(np.sin(2 * np.pi * f[:, None] * t[None, :] + ph[:, None]), 0) / 32
+        x[c] += rng.normal(0, 0.1, n)
+    x = x.astype(np.float32)
+    taps = ss.firwin(4095, [0.1, 0.3], window=("kaiser", 8.6), pass_zero=False).astype(np.float32)
+    rows = [0, 1, 64, 127, 128, 129]
+    ref = O.fir_mode_f64(x[rows].astype(np.float64), taps.astype(np.float64), int(S.FirMode.LFILTER))
+    xd, td = _dev(x, cuda), _dev(taps, cuda)
+    for prec in (S.Precision.BF16X3, S.Precision.BF16X6):
+        y = S.fir_batched(xd, td, S.FirMode.LFILTER, prec).cpu().numpy()
+        assert normwise_err(y[rows], ref) < 1e-5, prec
+
+
+def test_tensor_core_strided_and_repeat(cuda):
+    import torch
+    rng = np.random.default_rng(21)
+    big = rng.uniform(-1, 1, (140, 5004)).astype(np.float32)
+    taps = (rng.standard_normal(300) / 17).astype(np.float32)
+    xd = _dev(big, cuda)[:, :5000]
+    out = torch.zeros((140, 5100), device=cuda)[:, :5000]
+    ref = O.fir_mode_f64(big[:, :5000].astype(np.float64), taps.astype(np.float64),
+                         int(S.FirMode.REF_CORR))
+    for _ in range(2):  # the second call reuses the stream-ordered scratch pool
+        S.fir_batched(xd, _dev(taps, cuda), S.FirMode.REF_CORR, S.Precision.BF16X6, out=out)
+        assert normwise_err(out.cpu().numpy(), ref) < TOL_FP32
