@@ -264,6 +264,23 @@ SCIR_API int scir_sosfiltfilt_f64(const double* x, int64_t ld_x, int64_t batch,
                                   int padtype, int64_t padlen, int precision,
                                   double* y, int64_t ld_y, void* stream);
 
+/* scir_sosfiltfilt_f32 without any device allocation, for callers that may
+ * not allocate device memory while they filter: a real-time frame loop (an
+ * allocation can synchronise the device or stall behind other work and miss
+ * the frame), a process whose device memory is reserved up front by another
+ * pool, or an FFI host that forbids hidden allocations.  It has no
+ * counterpart in the reference.  The edge-extension scratch comes from a
+ * fixed file-scope device array of 4 Mi floats (16 MiB, held on every device
+ * that loads the library until the process exits); batch * padlen above that
+ * is rejected with SCIR_ERR_SHAPE.  The first call on a device looks the
+ * array's address up, so make it before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised by the
+ * caller.  Arguments and results are those of scir_sosfiltfilt_f32. */
+SCIR_API int scir_sosfiltfilt_f32_noalloc(const float* x, int64_t ld_x, int64_t batch,
+                                          int64_t n, const double* sos, int nsec,
+                                          int padtype, int64_t padlen, int precision,
+                                          float* y, int64_t ld_y, void* stream);
+
 /* ----------------------------------------------------------------------- */
 /* Host-buffer entry points with the reference's signatures (synchronous). */
 /* ----------------------------------------------------------------------- */

@@ -1,0 +1,134 @@
+// scir_sosfiltfilt_f32_noalloc: forward-backward SOS filtering that never
+// allocates device memory.
+//
+// Why it exists: some callers of this library cannot allocate device memory
+// at the moment they filter.  A real-time stream (audio, radar, sensor or SDR
+// frames every few milliseconds) must not call cudaMalloc/cudaMallocAsync on
+// its hot loop, because an allocation can synchronise the device, block
+// behind other work or fail under memory pressure and miss the frame
+// deadline.  Processes whose device memory is fully reserved up front by
+// another framework's pool, and foreign-language hosts that forbid hidden
+// allocations behind an FFI call, are in the same position.  This entry
+// point does the same work as scir_sosfiltfilt_f32 but takes its scratch (the
+// right-edge extension, batch x padlen floats) from a fixed file-scope device
+// array instead of the stream-ordered allocator.
+//
+// Limits and rules:
+//  - the array holds kNoallocScratchFloats floats (16 MiB); a call with
+//    batch * padlen above that is rejected with SCIR_ERR_SHAPE before any
+//    device work;
+//  - the array lives in every device that loads the library until the process
+//    exits;
+//  - the first call on a device looks up the array's device address with
+//    cudaGetSymbolAddress (once per device, with that device current); make
+//    that first call before any stream capture;
+//  - every call shares the one array: calls that overlap on the GPU (other
+//    streams, other host threads) race on it and must be serialised by the
+//    caller.  Nothing in it needs to start at zero: each call writes every
+//    scratch element it reads before reading it.
+#include "common.cuh"
+#include "kernels.cuh"
+
+#include <cstring>
+#include <mutex>
+
+namespace scir {
+namespace {
+
+constexpr size_t kNoallocScratchFloats = size_t(4) << 20;  // 16 MiB
+
+static __device__ __align__(256) float g_noalloc_scratch[kNoallocScratchFloats];
+
+constexpr int kMaxDev = 64;
+std::mutex g_noalloc_mutex;
+float* g_noalloc_ptr[kMaxDev] = {};
+
+// Device address of the array on the current device (looked up once).
+int noalloc_scratch(float** out) {
+    int dev = 0;
+    SCIR_CUDA_TRY(cudaGetDevice(&dev));
+    SCIR_REQUIRE(dev >= 0 && dev < kMaxDev, SCIR_ERR_NO_DEVICE, "device ordinal %d", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return set_error(SCIR_ERR_CUDA, "cudaGetSymbolAddress(noalloc scratch): %s",
+                             cudaGetErrorString(e));
+        }
+        g_noalloc_ptr[dev] = static_cast<float*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return SCIR_OK;
+}
+
+}  // namespace
+}  // namespace scir
+
+using namespace scir;
+
+extern "C" SCIR_API int scir_sosfiltfilt_f32_noalloc(const float* x, int64_t ld_x, int64_t batch,
+                                                     int64_t n, const double* sos, int nsec,
+                                                     int padtype, int64_t padlen, int precision,
+                                                     float* y, int64_t ld_y, void* stream) {
+    clear_error();
+    SCIR_REQUIRE(padtype == SCIR_PAD_NONE || padtype == SCIR_PAD_ODD, SCIR_ERR_INVALID_ARG,
+                 "unknown padtype %d", padtype);
+    SCIR_REQUIRE(sos != nullptr, SCIR_ERR_INVALID_ARG, "sos is NULL");
+    SCIR_REQUIRE(nsec >= 1 && nsec <= SCIR_SOS_MAX_SECTIONS, SCIR_ERR_INVALID_ARG,
+                 "nsec %d not in [1, %d]", nsec, SCIR_SOS_MAX_SECTIONS);
+    SCIR_REQUIRE(batch >= 0 && n >= 0, SCIR_ERR_INVALID_ARG, "negative batch or length");
+    SCIR_REQUIRE(ld_x >= n && ld_y >= n, SCIR_ERR_SHAPE, "row stride shorter than the row");
+    if (batch > 0 && n > 0) SCIR_REQUIRE(x && y, SCIR_ERR_INVALID_ARG, "NULL buffer");
+    SCIR_REQUIRE(y == x ? ld_y == ld_x : true, SCIR_ERR_INVALID_ARG,
+                 "in-place sosfiltfilt needs ld_y == ld_x");
+    int64_t edge = 0;
+    if (padtype == SCIR_PAD_ODD) edge = padlen < 0 ? sos_default_padlen(sos, nsec) : padlen;
+    SCIR_REQUIRE(edge >= 0, SCIR_ERR_INVALID_ARG, "negative padlen");
+    SCIR_REQUIRE(batch == 0 || n > edge, SCIR_ERR_SHAPE,
+                 "the signal must be longer than padlen (n=%lld, padlen=%lld)", (long long)n,
+                 (long long)edge);
+    SCIR_REQUIRE(edge == 0 || batch <= (int64_t)(kNoallocScratchFloats / (size_t)edge),
+                 SCIR_ERR_SHAPE,
+                 "batch * padlen = %lld * %lld exceeds the fixed scratch of %zu floats",
+                 (long long)batch, (long long)edge, kNoallocScratchFloats);
+    SosCoef c;
+    {
+        // the same coefficient block scir_sosfiltfilt_f32 builds (host memory only)
+        memset(&c, 0, sizeof(c));
+        c.nsec = nsec;
+        for (int s = 0; s < SCIR_SOS_MAX_SECTIONS; ++s) {
+            if (s < nsec) {
+                const double* r = sos + 6 * s;
+                c.c[s][0] = r[0];
+                c.c[s][1] = r[1];
+                c.c[s][2] = r[2];
+                c.c[s][3] = r[4];
+                c.c[s][4] = r[5];
+            } else {
+                c.c[s][0] = 1.0;
+            }
+            for (int j = 0; j < 5; ++j) c.cf[s][j] = (float)c.c[s][j];
+        }
+        if (padtype == SCIR_PAD_ODD) {
+            double zi[2 * SCIR_SOS_MAX_SECTIONS];
+            if (sos_zi_host(sos, nsec, zi) != SCIR_OK)
+                return set_error(SCIR_ERR_INVALID_ARG, "sosfilt_zi: a section has a pole at z=1");
+            for (int s = 0; s < nsec; ++s) {
+                c.zi[s][0] = zi[2 * s];
+                c.zi[s][1] = zi[2 * s + 1];
+            }
+        }
+    }
+    const DeviceInfo* info = nullptr;
+    int rc = current_device(&info);
+    if (rc) return rc;
+    float* tail = nullptr;
+    rc = noalloc_scratch(&tail);
+    if (rc) return rc;
+    if (batch == 0 || n == 0) return SCIR_OK;
+    return launch_sosfiltfilt<float>(x, ld_x, batch, n, c, edge, padtype == SCIR_PAD_ODD,
+                                     precision, y, ld_y, edge > 0 ? tail : nullptr,
+                                     as_stream(stream));
+}
