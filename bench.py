@@ -182,7 +182,7 @@ class Resample(Workload):
         self.n_out = S.resample_poly_out_len(self.N, self.UP, self.DOWN)
         self.y = torch.empty((self.B, self.n_out), device=dev)
         self.kh = S.resample_poly_default_taps(self.UP, self.DOWN).size
-        self.kernel = "poly_fast_kernel"
+        self.kernel = "poly_stream_kernel"
 
     @classmethod
     def config(cls):
@@ -793,7 +793,7 @@ def run_ours(args):
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded torch.randn on the device)",
-        "config": dict(W.config(), channels=W.B, precision=prec.name,
+        "config": dict(W.config(), channels=getattr(W, "B", None), precision=prec.name,
                        parallelism=f"replicas x{world}"),
         "roofline": {"bound": W.bound, "achieved": achieved, "peak": peak, "unit": unit,
                      "frac": achieved / peak, "traffic": traffic,

@@ -97,11 +97,17 @@ typedef enum scir_precision {
  *   operation order without FMA (crates/scir-iir-filters/src/filter.rs:
  *   50-61): bit-identical to the reference for f64 data.
  * SCIR_SOS_FP64: FP64 coefficients and state with FMA.
- * SCIR_SOS_FP32: coefficients rounded to FP32, FP32 state. */
+ * SCIR_SOS_FP32: coefficients rounded to FP32, FP32 state (DF2T).
+ * SCIR_SOS_FP32_COUPLED: FP32 state, each complex-pole section in coupled
+ *   (modal) form driven by increments whose coefficients (sigma-1, omega)
+ *   were computed in FP64, so poles near the unit circle are not moved by
+ *   FP32 rounding; real-pole sections run FP32 DF2T.  States in and out are
+ *   DF2T states, as in every other mode. */
 typedef enum scir_sos_precision {
     SCIR_SOS_FP64_EXACT = 0,
     SCIR_SOS_FP64 = 1,
-    SCIR_SOS_FP32 = 2
+    SCIR_SOS_FP32 = 2,
+    SCIR_SOS_FP32_COUPLED = 3
 } scir_sos_precision;
 
 /* Edge extension for sosfiltfilt (SciPy padtype). */

@@ -52,9 +52,10 @@ class Precision(enum.IntEnum):
 
 
 class SosPrecision(enum.IntEnum):
-    FP64_EXACT = 0  # FP64 state + coefficients, reference operation order
-    FP64 = 1        # FP64 state + coefficients, FMA
-    FP32 = 2        # all FP32
+    FP64_EXACT = 0    # FP64 state + coefficients, reference operation order
+    FP64 = 1          # FP64 state + coefficients, FMA
+    FP32 = 2          # all FP32 (DF2T)
+    FP32_COUPLED = 3  # FP32 state, complex-pole sections in coupled form (FP64-derived)
 
 
 class PadType(enum.IntEnum):

@@ -139,30 +139,8 @@ int fill_sos(const double* sos, int nsec, bool want_zi, SosCoef* c) {
     SCIR_REQUIRE(sos != nullptr, SCIR_ERR_INVALID_ARG, "sos is NULL");
     SCIR_REQUIRE(nsec >= 1 && nsec <= SCIR_SOS_MAX_SECTIONS, SCIR_ERR_INVALID_ARG,
                  "nsec %d not in [1, %d]", nsec, SCIR_SOS_MAX_SECTIONS);
-    memset(c, 0, sizeof(*c));
-    c->nsec = nsec;
-    for (int s = 0; s < SCIR_SOS_MAX_SECTIONS; ++s) {
-        if (s < nsec) {
-            const double* r = sos + 6 * s;
-            c->c[s][0] = r[0];
-            c->c[s][1] = r[1];
-            c->c[s][2] = r[2];
-            c->c[s][3] = r[4];
-            c->c[s][4] = r[5];
-        } else {
-            c->c[s][0] = 1.0;  // identity section: out = prev
-        }
-        for (int j = 0; j < 5; ++j) c->cf[s][j] = (float)c->c[s][j];
-    }
-    if (want_zi) {
-        double zi[2 * SCIR_SOS_MAX_SECTIONS];
-        if (sos_zi_host(sos, nsec, zi) != SCIR_OK)
-            return set_error(SCIR_ERR_INVALID_ARG, "sosfilt_zi: a section has a pole at z=1 or a0=0");
-        for (int s = 0; s < nsec; ++s) {
-            c->zi[s][0] = zi[2 * s];
-            c->zi[s][1] = zi[2 * s + 1];
-        }
-    }
+    if (build_sos_coef(sos, nsec, want_zi, c) != SCIR_OK)
+        return set_error(SCIR_ERR_INVALID_ARG, "sosfilt_zi: a section has a pole at z=1 or a0=0");
     return SCIR_OK;
 }
 

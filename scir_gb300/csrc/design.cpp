@@ -9,9 +9,14 @@
 // - sos_zi_host: scipy.signal.sosfilt_zi (per-section lfilter_zi in closed
 //   form, scaled by the DC gain of the preceding sections).
 // - sos_default_padlen: SciPy's filtfilt edge for an SOS cascade.
+// - build_sos_coef: the kernel-parameter block of an SOS cascade, including
+//   the coupled (modal) form of every complex-pole section and the maps
+//   between its state and the DF2T state, all computed in FP64.
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 
+#include "kernels.cuh"
 #include "scir_gb300.h"
 
 namespace scir {
@@ -97,6 +102,77 @@ int64_t sos_default_padlen(const double* sos, int nsec) {
         if (sos[6 * s + 5] == 0.0) ++za;
     }
     return 3 * (int64_t)(2 * nsec + 1 - (zb < za ? zb : za));
+}
+
+}  // namespace scir
+
+namespace scir {
+
+// Coupled form of H(z) = (b0 + b1 z^-1 + b2 z^-2) / (1 + a1 z^-1 + a2 z^-2)
+// with complex poles sigma +- i omega:
+//   state s = (u, v), s' = A s + [1, 0]^T x, A = [[sigma, -omega], [omega, sigma]],
+//   y = C s + b0 x,  C = (b1 - a1 b0, (b2 - a2 b0 + C1 sigma) / omega),
+// which has the same transfer function (the denominator of C (zI - A)^-1 B
+// is z^2 + a1 z + a2).  Zero-input responses match DF2T when
+// [C; CA] s = (s1, s2 - a1 s1), which gives the two state maps.
+int build_sos_coef(const double* sos, int nsec, bool want_zi, SosCoef* c) {
+    memset(c, 0, sizeof(*c));
+    c->nsec = nsec;
+    for (int s = 0; s < SCIR_SOS_MAX_SECTIONS; ++s) {
+        if (s < nsec) {
+            const double* r = sos + 6 * s;
+            c->c[s][0] = r[0];
+            c->c[s][1] = r[1];
+            c->c[s][2] = r[2];
+            c->c[s][3] = r[4];
+            c->c[s][4] = r[5];
+        } else {
+            c->c[s][0] = 1.0;  // identity section: out = prev
+        }
+        for (int j = 0; j < 5; ++j) c->cf[s][j] = (float)c->c[s][j];
+        if (s >= nsec) continue;
+        const double b0 = c->c[s][0], b1 = c->c[s][1], b2 = c->c[s][2];
+        const double a1 = c->c[s][3], a2 = c->c[s][4];
+        const double disc = a1 * a1 - 4.0 * a2;
+        if (!(disc < 0.0)) continue;  // real poles: DF2T
+        const double sigma = -0.5 * a1, omega = 0.5 * std::sqrt(-disc);
+        const double C1 = b1 - a1 * b0;
+        const double C2 = (b2 - a2 * b0 + C1 * sigma) / omega;
+        const double o00 = C1, o01 = C2;
+        const double o10 = C1 * sigma + C2 * omega, o11 = -C1 * omega + C2 * sigma;
+        const double det = o00 * o11 - o01 * o10;
+        const double scale = std::fabs(o00 * o11) + std::fabs(o01 * o10);
+        if (!(std::fabs(det) > 1e-12 * scale) || !std::isfinite(det)) continue;
+        const double i00 = o11 / det, i01 = -o01 / det, i10 = -o10 / det, i11 = o00 / det;
+        // (u, v) = O^-1 (s1, s2 - a1 s1)
+        c->to_cp[s][0] = i00 - a1 * i01;
+        c->to_cp[s][1] = i01;
+        c->to_cp[s][2] = i10 - a1 * i11;
+        c->to_cp[s][3] = i11;
+        // (s1, s2) = (O0 s, O1 s + a1 O0 s)
+        c->from_cp[s][0] = o00;
+        c->from_cp[s][1] = o01;
+        c->from_cp[s][2] = o10 + a1 * o00;
+        c->from_cp[s][3] = o11 + a1 * o01;
+        c->cp[s][0] = (float)(-0.5 * a1 - 1.0);  // sigma - 1, exact in FP64
+        c->cp[s][1] = (float)omega;
+        c->cp[s][2] = (float)C1;
+        c->cp[s][3] = (float)C2;
+        c->cp[s][4] = (float)b0;
+        c->coupled[s] = 1;
+    }
+    if (want_zi) {
+        double zi[2 * SCIR_SOS_MAX_SECTIONS];
+        if (sos_zi_host(sos, nsec, zi) != SCIR_OK) return SCIR_ERR_INVALID_ARG;
+        for (int s = 0; s < nsec; ++s) {
+            c->zi[s][0] = zi[2 * s];
+            c->zi[s][1] = zi[2 * s + 1];
+            const double* m = c->to_cp[s];
+            c->zc[s][0] = m[0] * zi[2 * s] + m[1] * zi[2 * s + 1];
+            c->zc[s][1] = m[2] * zi[2 * s] + m[3] * zi[2 * s + 1];
+        }
+    }
+    return SCIR_OK;
 }
 
 }  // namespace scir

@@ -48,8 +48,18 @@ struct SosCoef {
     double c[SCIR_SOS_MAX_SECTIONS][5];  // b0 b1 b2 a1 a2 (a0 taken as 1); unused = identity
     float cf[SCIR_SOS_MAX_SECTIONS][5];  // the same rounded to FP32
     double zi[SCIR_SOS_MAX_SECTIONS][2]; // sosfilt_zi (filtfilt with padding)
+    // Coupled (modal) form of complex-pole sections, all from FP64 on the host:
+    //   y = c1*u + c2*v + d*x;  u += (sigma-1)*u - omega*v + x;  v += omega*u + (sigma-1)*v
+    float cp[SCIR_SOS_MAX_SECTIONS][5];  // sigma-1, omega, c1, c2, d
+    int coupled[SCIR_SOS_MAX_SECTIONS];  // 0: real poles, the section runs DF2T in FP32
+    double to_cp[SCIR_SOS_MAX_SECTIONS][4];   // DF2T state (s1, s2) -> coupled (u, v), row-major
+    double from_cp[SCIR_SOS_MAX_SECTIONS][4]; // coupled (u, v) -> DF2T state (s1, s2)
+    double zc[SCIR_SOS_MAX_SECTIONS][2];      // zi in coupled coordinates
     int nsec;
 };
+
+// Fills every field of SosCoef from a host [nsec][6] SOS matrix.
+int build_sos_coef(const double* sos, int nsec, bool want_zi, SosCoef* c);
 template <typename T>
 int launch_sosfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const SosCoef& c,
                    const double* zi, double* zf, int precision, T* y, int64_t ld_y,

@@ -29,7 +29,6 @@
 #include "common.cuh"
 #include "kernels.cuh"
 
-#include <cstring>
 #include <mutex>
 
 namespace scir {
@@ -93,34 +92,9 @@ extern "C" SCIR_API int scir_sosfiltfilt_f32_noalloc(const float* x, int64_t ld_
                  SCIR_ERR_SHAPE,
                  "batch * padlen = %lld * %lld exceeds the fixed scratch of %zu floats",
                  (long long)batch, (long long)edge, kNoallocScratchFloats);
-    SosCoef c;
-    {
-        // the same coefficient block scir_sosfiltfilt_f32 builds (host memory only)
-        memset(&c, 0, sizeof(c));
-        c.nsec = nsec;
-        for (int s = 0; s < SCIR_SOS_MAX_SECTIONS; ++s) {
-            if (s < nsec) {
-                const double* r = sos + 6 * s;
-                c.c[s][0] = r[0];
-                c.c[s][1] = r[1];
-                c.c[s][2] = r[2];
-                c.c[s][3] = r[4];
-                c.c[s][4] = r[5];
-            } else {
-                c.c[s][0] = 1.0;
-            }
-            for (int j = 0; j < 5; ++j) c.cf[s][j] = (float)c.c[s][j];
-        }
-        if (padtype == SCIR_PAD_ODD) {
-            double zi[2 * SCIR_SOS_MAX_SECTIONS];
-            if (sos_zi_host(sos, nsec, zi) != SCIR_OK)
-                return set_error(SCIR_ERR_INVALID_ARG, "sosfilt_zi: a section has a pole at z=1");
-            for (int s = 0; s < nsec; ++s) {
-                c.zi[s][0] = zi[2 * s];
-                c.zi[s][1] = zi[2 * s + 1];
-            }
-        }
-    }
+    SosCoef c;  // host memory only
+    if (build_sos_coef(sos, nsec, padtype == SCIR_PAD_ODD, &c) != SCIR_OK)
+        return set_error(SCIR_ERR_INVALID_ARG, "sosfilt_zi: a section has a pole at z=1");
     const DeviceInfo* info = nullptr;
     int rc = current_device(&info);
     if (rc) return rc;

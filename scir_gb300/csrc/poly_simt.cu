@@ -31,6 +31,11 @@
 #include "sm100.cuh"
 
 #include <algorithm>
+#include <array>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 namespace scir {
 namespace {
@@ -330,7 +335,23 @@ int try_stream(const PolyArgs& a, cudaStream_t st) {
     g.n_periods = ceil_div(a.n_out, a.up);
     g.items_per_row = ceil_div(g.n_periods, g.IP);
     g.n_items = g.items_per_row * a.batch;
-    assign_lanes(g, maxrel);
+    {
+        // the lane assignment depends only on the filter geometry: search once
+        using Key = std::tuple<int, int, int64_t, int>;
+        static std::mutex mu;
+        static std::map<Key, std::array<uint8_t, kNW * 32>> cache;
+        const Key key{a.up, a.down, a.off, g.Q};
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if (it == cache.end()) {
+            assign_lanes(g, maxrel);
+            std::array<uint8_t, kNW * 32> units;
+            memcpy(units.data(), g.unit, sizeof(g.unit));
+            cache.emplace(key, units);
+        } else {
+            memcpy(g.unit, it->second.data(), sizeof(g.unit));
+        }
+    }
     switch (P) {
     case 1: return dispatch_jwa<1>(a, g, jwa_b, st);
     case 2: return dispatch_jwa<2>(a, g, jwa_b, st);

@@ -15,7 +15,13 @@
 // PREC 0 (FP64_EXACT) rounds every product and sum separately in the
 // reference's order: for f64 data the result is bit-identical to the
 // reference.  PREC 1 uses FP64 FMA.  PREC 2 rounds the coefficients to FP32
-// and keeps an FP32 state.
+// and keeps an FP32 state.  PREC 3 (FP32_COUPLED) runs each complex-pole
+// section in coupled (modal) form with FP32 state: the state matrix
+// [[sigma, -omega], [omega, sigma]] is applied as an increment with
+// coefficients sigma-1 and omega that were computed in FP64, so the poles
+// stay where FP64 puts them (a1, a2 rounded to FP32 move a pole 2e-4 from the
+// unit circle by ~10 % of that distance); real-pole sections run FP32 DF2T.
+// Initial and final states are exchanged in DF2T coordinates.
 //
 // sosfiltfilt (SciPy semantics with odd padding, or the reference's unpadded
 // forward-backward) runs both passes in one thread per channel:
@@ -41,6 +47,8 @@ template <int PREC>
 struct AccT { using type = double; };
 template <>
 struct AccT<2> { using type = float; };
+template <>
+struct AccT<3> { using type = float; };
 
 // Coefficients are read from the kernel-parameter bank (sc is a __grid_constant__
 // parameter), so they cost no registers; sections past nsec hold b0 = 1.
@@ -60,14 +68,54 @@ __device__ __forceinline__ A sos_step(const SosCoef& sc, A (&s1)[NS], A (&s2)[NS
             out = fma(c[0], prev, s1[s]);
             s1[s] = fma(-c[3], out, fma(c[1], prev, s2[s]));
             s2[s] = fma(-c[4], out, c[2] * prev);
-        } else {
+        } else if constexpr (PREC == 2) {
             const float* c = sc.cf[s];
             out = fmaf(c[0], prev, s1[s]);
             s1[s] = fmaf(-c[3], out, fmaf(c[1], prev, s2[s]));
             s2[s] = fmaf(-c[4], out, c[2] * prev);
+        } else {
+            if (sc.coupled[s]) {
+                const float* k = sc.cp[s];
+                const float u = s1[s], v = s2[s];
+                out = fmaf(k[2], u, fmaf(k[3], v, k[4] * prev));
+                s1[s] = u + fmaf(k[0], u, fmaf(-k[1], v, prev));
+                s2[s] = v + fmaf(k[1], u, k[0] * v);
+            } else {
+                const float* c = sc.cf[s];
+                out = fmaf(c[0], prev, s1[s]);
+                s1[s] = fmaf(-c[3], out, fmaf(c[1], prev, s2[s]));
+                s2[s] = fmaf(-c[4], out, c[2] * prev);
+            }
         }
     }
     return out;
+}
+
+// DF2T state (s1, s2) of section s in the kernel's own coordinates.
+template <int PREC, typename A>
+__device__ __forceinline__ void state_in(const SosCoef& sc, int s, double s1, double s2, A& o1,
+                                         A& o2) {
+    if (PREC == 3 && sc.coupled[s]) {
+        const double* m = sc.to_cp[s];
+        o1 = (A)(m[0] * s1 + m[1] * s2);
+        o2 = (A)(m[2] * s1 + m[3] * s2);
+    } else {
+        o1 = (A)s1;
+        o2 = (A)s2;
+    }
+}
+
+template <int PREC, typename A>
+__device__ __forceinline__ void state_out(const SosCoef& sc, int s, A i1, A i2, double& s1,
+                                          double& s2) {
+    if (PREC == 3 && sc.coupled[s]) {
+        const double* m = sc.from_cp[s];
+        s1 = m[0] * (double)i1 + m[1] * (double)i2;
+        s2 = m[2] * (double)i1 + m[3] * (double)i2;
+    } else {
+        s1 = (double)i1;
+        s2 = (double)i2;
+    }
 }
 
 // Loads tile [t0, t0+32) of 32 rows starting at row r0 into registers
@@ -112,10 +160,9 @@ sosfilt_kernel(const T* __restrict__ x, int64_t ld_x, int64_t batch, int64_t n,
     for (int k = 0; k < NS; ++k) {
         s1[k] = A(0);
         s2[k] = A(0);
-        if (zi && ch < batch && k < sc.nsec) {
-            s1[k] = (A)zi[(ch * sc.nsec + k) * 2 + 0];
-            s2[k] = (A)zi[(ch * sc.nsec + k) * 2 + 1];
-        }
+        if (zi && ch < batch && k < sc.nsec)
+            state_in<PREC>(sc, k, zi[(ch * sc.nsec + k) * 2 + 0], zi[(ch * sc.nsec + k) * 2 + 1],
+                           s1[k], s2[k]);
     }
     T nxt[kTT];
     tile_fetch(nxt, x, ld_x, r0, batch, n, 0, lane);
@@ -134,9 +181,14 @@ sosfilt_kernel(const T* __restrict__ x, int64_t ld_x, int64_t batch, int64_t n,
         __syncwarp();
     }
     if (zf && ch < batch) {
-        for (int k = 0; k < sc.nsec; ++k) {
-            zf[(ch * sc.nsec + k) * 2 + 0] = (double)s1[k];
-            zf[(ch * sc.nsec + k) * 2 + 1] = (double)s2[k];
+#pragma unroll
+        for (int k = 0; k < NS; ++k) {
+            if (k < sc.nsec) {
+                double o1, o2;
+                state_out<PREC>(sc, k, s1[k], s2[k], o1, o2);
+                zf[(ch * sc.nsec + k) * 2 + 0] = o1;
+                zf[(ch * sc.nsec + k) * 2 + 1] = o2;
+            }
         }
     }
 }
@@ -168,8 +220,9 @@ sosfiltfilt_kernel(const T* __restrict__ x, int64_t ld_x, int64_t batch, int64_t
 #pragma unroll
         for (int k = 0; k < NS; ++k) {
             const bool on = k < sc.nsec && use_zi;
-            s1[k] = on ? (A)sc.zi[k][0] * e0 : A(0);
-            s2[k] = on ? (A)sc.zi[k][1] * e0 : A(0);
+            const double* z = (PREC == 3 && sc.coupled[k]) ? sc.zc[k] : sc.zi[k];
+            s1[k] = on ? (A)(z[0] * (double)e0) : A(0);
+            s2[k] = on ? (A)(z[1] * (double)e0) : A(0);
         }
         for (int64_t j = 0; j < edge; ++j) {
             const A e = A(2) * xl - (live ? (A)xr[edge - j] : A(0));
@@ -207,8 +260,9 @@ sosfiltfilt_kernel(const T* __restrict__ x, int64_t ld_x, int64_t batch, int64_t
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
         const bool on = k < sc.nsec && use_zi;
-        s1[k] = on ? (A)sc.zi[k][0] * ylast : A(0);
-        s2[k] = on ? (A)sc.zi[k][1] * ylast : A(0);
+        const double* z = (PREC == 3 && sc.coupled[k]) ? sc.zc[k] : sc.zi[k];
+        s1[k] = on ? (A)(z[0] * (double)ylast) : A(0);
+        s2[k] = on ? (A)(z[1] * (double)ylast) : A(0);
     }
     for (int64_t i = edge - 1; i >= 0; --i) {
         const A e = live ? (A)tail[i * batch + ch] : A(0);
@@ -287,6 +341,8 @@ int launch_sosfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const Sos
     case SCIR_SOS_FP64_EXACT: return dispatch_sosfilt<T, 0>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st);
     case SCIR_SOS_FP64: return dispatch_sosfilt<T, 1>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st);
     case SCIR_SOS_FP32: return dispatch_sosfilt<T, 2>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st);
+    case SCIR_SOS_FP32_COUPLED:
+        return dispatch_sosfilt<T, 3>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st);
     default: return set_error(SCIR_ERR_INVALID_ARG, "unknown SOS precision %d", precision);
     }
 }
@@ -303,6 +359,8 @@ int launch_sosfiltfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const
         return dispatch_sosfiltfilt<T, 1>(x, ld_x, batch, n, c, edge, use_zi, y, ld_y, tail, st);
     case SCIR_SOS_FP32:
         return dispatch_sosfiltfilt<T, 2>(x, ld_x, batch, n, c, edge, use_zi, y, ld_y, tail, st);
+    case SCIR_SOS_FP32_COUPLED:
+        return dispatch_sosfiltfilt<T, 3>(x, ld_x, batch, n, c, edge, use_zi, y, ld_y, tail, st);
     default: return set_error(SCIR_ERR_INVALID_ARG, "unknown SOS precision %d", precision);
     }
 }

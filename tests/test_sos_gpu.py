@@ -120,3 +120,44 @@ def test_short_signal_rejected(cuda):
     with pytest.raises(S.GpuError) as ei:
         S.sosfiltfilt_f64(SOS5, x)
     assert ei.value.kind == "ShapeMismatch"
+
+
+# ---------------------------------------------------------------- coupled form
+# FP32 state in coupled (modal) form with FP64-derived increments: <= 1e-5
+# normwise vs the FP64 oracle on the near-unit-circle band-pass (cfg 5).
+def test_cfg5_coupled_fp32(cuda):
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((96, 131072)).astype(np.float32)
+    ref = O.sosfilt_f64(SOS5, x.astype(np.float64))
+    y = S.sosfilt_f32(SOS5, _dev(x, cuda), precision=S.SosPrecision.FP32_COUPLED).cpu().numpy()
+    assert normwise_err(y, ref) < TOL
+
+
+@pytest.mark.parametrize("sos", [ss.butter(5, 0.2, output="sos"),            # a real-pole section
+                                 ss.cheby1(6, 1, [0.1, 0.3], btype="bandpass", output="sos"),
+                                 ss.butter(4, 0.3, btype="highpass", output="sos")])
+def test_coupled_general_filters(cuda, sos):
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((40, 20000)).astype(np.float32)
+    ref = O.sosfilt_f64(sos, x.astype(np.float64))
+    y = S.sosfilt_f32(sos, _dev(x, cuda), precision=S.SosPrecision.FP32_COUPLED).cpu().numpy()
+    assert normwise_err(y, ref) < TOL
+
+
+def test_coupled_state_chaining_and_filtfilt(cuda):
+    import torch
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal((33, 30000)).astype(np.float32)
+    xd = _dev(x, cuda)
+    P = S.SosPrecision.FP32_COUPLED
+    zi = rng.standard_normal((33, 8, 2)) * 0.01
+    y1, zf = S.sosfilt_f32(SOS5, xd[:, :12000].contiguous(), zi=_dev(zi, cuda), return_zf=True,
+                           precision=P)
+    y2 = S.sosfilt_f32(SOS5, xd[:, 12000:].contiguous(), zi=zf, precision=P)
+    full = torch.cat([y1, y2], 1).cpu().numpy()
+    ref = O.sosfilt_f64(SOS5, x.astype(np.float64), zi=zi)
+    assert normwise_err(full, ref) < TOL
+    ref_zf = O.sosfilt_f64(SOS5, x[:, :12000].astype(np.float64), zi=zi, return_zf=True)[1]
+    assert np.max(np.abs(zf.cpu().numpy() - ref_zf)) < 1e-4 * np.max(np.abs(ref_zf))
+    yff = S.sosfiltfilt_f32(SOS5, xd, precision=P).cpu().numpy()
+    assert normwise_err(yff, O.sosfiltfilt_f64(SOS5, x.astype(np.float64))) < TOL
