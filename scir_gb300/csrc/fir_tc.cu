@@ -12,20 +12,23 @@
 // layout with a 16-byte leading (K) offset and a 128-byte stride (N) offset,
 // so every B_phi is a descriptor pointing into a contiguous tap window in
 // shared memory -- no im2col, no Toeplitz materialisation.  The 8 phases of
-// one tile are 8 MMAs of N = U writing adjacent TMEM column ranges.
+// one tile are 8 MMAs of N = U writing adjacent TMEM column ranges; with
+// U = 64 a tile is 512 outputs and fills the 512 TMEM columns.
 //
 // Precision.  x and c are split into bf16 terms (x = x1 + x2 [+ x3]) by a
 // prep pass into scratch memory; BF16X3 accumulates x1c1 + x1c2 + x2c1, BF16X6
-// adds x1c3 + x2c2 + x3c1.  x1c1 and the cross terms accumulate in FP32 in two
-// separate TMEM accumulators (measured: mixing them in one accumulator
-// doubles to quadruples the error on 4,095-tap filters).
+// adds x1c3 + x2c2 + x3c1.  The dominant x1c1 and the cross terms are two
+// passes of the kernel with their own FP32 accumulators: pass 0 writes x1c1,
+// pass 1 adds the cross-term sum to it in the epilogue (measured: mixing
+// them in one accumulator doubles to quadruples the error on 4,095-tap
+// filters).
 //
 // Roles (192 threads, one CTA per SM, persistent over tiles):
-//   warp 0    TMA producer: signal box + 8 phase tap windows per K chunk of 64
-//             into an N-stage ring (full/empty mbarriers);
+//   warp 0    TMA producer: signal box(es) + 8 phase tap windows per term and
+//             K chunk of 64 into an N-stage ring (full/empty mbarriers);
 //   warp 1    one thread issues the MMAs and commits stages and tiles;
-//   warps 2-5 epilogue: tcgen05.ld of the two accumulators of a tile, FP32
-//             sum, phase interleave in registers, 16-byte stores.
+//   warps 2-5 epilogue: tcgen05.ld of the accumulator, phase interleave in
+//             registers, 16-byte stores (pass 1: load, add, store).
 // Every wait is bounded; a timeout sets the device error word, the CTA
 // leaves its loops, frees its TMEM and exits.
 #include "common.cuh"
@@ -92,22 +95,29 @@ __global__ void split_taps_kernel(const float* __restrict__ taps, int64_t k, int
     }
 }
 
-// (signal term, tap term) of product p
-__device__ __forceinline__ int prod_a(int p) { return (p == 0 || p == 1 || p == 3) ? 0 : (p == 5 ? 2 : 1); }
-__device__ __forceinline__ int prod_b(int p) { return (p == 0 || p == 2 || p == 5) ? 0 : (p == 3 ? 2 : 1); }
+// Products of a pass as (signal term, tap term).  Pass 0 is the dominant
+// x1*c1; pass 1 is the cross terms x1c2, x2c1 (BF16X3) and x1c3, x2c2, x3c1
+// (BF16X6 adds them).  Each pass accumulates in its own TMEM accumulator;
+// pass 1's epilogue adds its sum to pass 0's output in FP32.  Cross terms
+// added into the large x1*c1 sum would be rounded against its magnitude;
+// kept apart they are rounded against their own, 2^-8 smaller, one.
+template <int PASS>
+__device__ __forceinline__ int prod_a(int p) {
+    return PASS == 0 ? 0 : (p == 0 ? 0 : p == 1 ? 1 : p == 2 ? 0 : p == 3 ? 1 : 2);
+}
+template <int PASS>
+__device__ __forceinline__ int prod_b(int p) {
+    return PASS == 0 ? 0 : (p == 0 ? 1 : p == 1 ? 0 : p == 2 ? 2 : p == 3 ? 1 : 0);
+}
 
-template <int U, int TERMS, int NPROD>
+template <int U, int TA, int TB, int PASS, int NPROD>
 __global__ void __launch_bounds__(kThreads, 1)
 fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __restrict__ G,
               const TcGeom g, float* __restrict__ y, int64_t ld_y, unsigned* __restrict__ err) {
     constexpr int NCOL = kPh * U;                      // accumulator columns per tile
-    // Two accumulators per tile, summed in FP32 by the epilogue: slot 0 takes
-    // the dominant x1*c1 products, slot 1 every cross term.  Cross terms added
-    // into the large slot-0 sum would be rounded against its magnitude; kept
-    // apart they are rounded against their own (2^-8 smaller) one.
-    constexpr int NSLOT = 2;
-    constexpr int NACC = (kTmemCols / (NCOL * NSLOT)) >= 2 ? 2 : 1;
+    constexpr int NACC = (kTmemCols / NCOL) >= 2 ? 2 : 1;  // tiles in flight in TMEM
     constexpr int WB = kKC + 8 * U;                    // tap window per phase per chunk
+    constexpr uint32_t kABytes = TA * kABytesTerm;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     uint64_t* full = reinterpret_cast<uint64_t*>(base + (size_t)g.nstage * g.stage_bytes);
@@ -157,12 +167,12 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
                     uint8_t* sb = base + (size_t)st * g.stage_bytes;
                     mbar_arrive_expect_tx(&full[st], g.tx_bytes);
 #pragma unroll
-                    for (int t = 0; t < TERMS; ++t)
+                    for (int t = 0; t < TA; ++t)
                         tma_load_3d(sb + t * kABytesTerm, &amap, &full[st],
                                     (int32_t)(xc0 + (int64_t)c * kKC), (int32_t)(cg * kM), t);
-                    uint8_t* bb = sb + TERMS * kABytesTerm;
+                    uint8_t* bb = sb + kABytes;
 #pragma unroll
-                    for (int t = 0; t < TERMS; ++t)
+                    for (int t = 0; t < TB; ++t)
                         for (int phz = 0; phz < kPh; ++phz)
                             bulk_load(bb + (t * kPh + phz) * WB * 2,
                                       G + ((int64_t)(t * kPh + phz) * g.LG + (int64_t)c * kKC),
@@ -183,7 +193,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
                     break;
                 }
                 tc_fence_after();
-                const uint32_t dbase = tmem + (uint32_t)(a * NCOL * NSLOT);
+                const uint32_t dbase = tmem + (uint32_t)(a * NCOL);
                 for (int c = 0; c < g.nchunks; ++c, ++it) {
                     const int st = (int)(it % (uint32_t)g.nstage);
                     const uint32_t ph = (it / (uint32_t)g.nstage) & 1u;
@@ -197,7 +207,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
                     // operands through compile-time offsets (encoded in 16-byte units)
                     const uint32_t sa = smem_u32(base + (size_t)st * g.stage_bytes);
                     const uint64_t ad0 = smem_desc(sa, 16, 1024, 2);
-                    const uint64_t bd0 = smem_desc(sa + TERMS * kABytesTerm, 16, 128, 0);
+                    const uint64_t bd0 = smem_desc(sa + kABytes, 16, 128, 0);
                     const uint32_t acc_c = c != 0 ? 1u : 0u;
 #pragma unroll
                     for (int ks = 0; ks < kKC / 16; ++ks) {
@@ -205,16 +215,12 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
                         for (int phz = 0; phz < kPh; ++phz) {
 #pragma unroll
                             for (int p = 0; p < NPROD; ++p) {
-                                const int ta = prod_a(p), tb = prod_b(p);
-                                const uint64_t ad =
-                                    ad0 + (uint64_t)((ta * kABytesTerm + ks * 32) >> 4);
-                                const uint64_t bd =
-                                    bd0 + (uint64_t)(((tb * kPh + phz) * WB * 2 + ks * 32) >> 4);
-                                const int slot = p == 0 ? 0 : 1;
-                                // first product into each slot of the tile overwrites it
-                                const bool first_k = ks == 0 && (p == 0 || p == 1);
-                                tc_mma_f16(dbase + (uint32_t)(slot * NCOL) + phz * U, ad, bd, idesc,
-                                           first_k ? acc_c : 1u);
+                                const uint64_t ad = ad0 + (uint64_t)(
+                                    (prod_a<PASS>(p) * kABytesTerm + ks * 32) >> 4);
+                                const uint64_t bd = bd0 + (uint64_t)(
+                                    ((prod_b<PASS>(p) * kPh + phz) * WB * 2 + ks * 32) >> 4);
+                                tc_mma_f16(dbase + phz * U, ad, bd, idesc,
+                                           (ks == 0 && p == 0) ? acc_c : 1u);
                             }
                         }
                     }
@@ -240,22 +246,12 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
             const int64_t row = cg * kM + q * 32 + lane;
             const int64_t o0 = blk * NCOL;
             float* __restrict__ yr = y + row * ld_y;
-            const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * NCOL * NSLOT);
+            const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * NCOL);
 #pragma unroll 1
             for (int u0 = 0; u0 < U; u0 += 16) {
                 float v[kPh][16];
 #pragma unroll
                 for (int phz = 0; phz < kPh; ++phz) tmem_ld16(tb + phz * U + u0, v[phz]);
-                {
-                    float w[kPh][16];
-#pragma unroll
-                    for (int phz = 0; phz < kPh; ++phz) tmem_ld16(tb + NCOL + phz * U + u0, w[phz]);
-                    tmem_wait_ld();
-#pragma unroll
-                    for (int phz = 0; phz < kPh; ++phz)
-#pragma unroll
-                        for (int i = 0; i < 16; ++i) v[phz][i] += w[phz][i];
-                }
                 tmem_wait_ld();
                 if (row < g.batch) {
 #pragma unroll
@@ -264,12 +260,20 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
                         const int64_t o = o0 + 8 * u;
                         if (g.vec_store && o + 8 <= g.n_out) {
                             float4* p4 = reinterpret_cast<float4*>(yr + o);
-                            p4[0] = make_float4(v[0][i], v[1][i], v[2][i], v[3][i]);
-                            p4[1] = make_float4(v[4][i], v[5][i], v[6][i], v[7][i]);
+                            float4 lo = make_float4(v[0][i], v[1][i], v[2][i], v[3][i]);
+                            float4 hi = make_float4(v[4][i], v[5][i], v[6][i], v[7][i]);
+                            if (PASS == 1) {
+                                const float4 plo = p4[0], phi = p4[1];
+                                lo.x += plo.x; lo.y += plo.y; lo.z += plo.z; lo.w += plo.w;
+                                hi.x += phi.x; hi.y += phi.y; hi.z += phi.z; hi.w += phi.w;
+                            }
+                            p4[0] = lo;
+                            p4[1] = hi;
                         } else {
 #pragma unroll
                             for (int phz = 0; phz < kPh; ++phz)
-                                if (o + phz < g.n_out) yr[o + phz] = v[phz][i];
+                                if (o + phz < g.n_out)
+                                    yr[o + phz] = PASS == 1 ? yr[o + phz] + v[phz][i] : v[phz][i];
                         }
                     }
                 }
@@ -285,7 +289,37 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
     }
 }
 
-template <int U, int TERMS, int NPROD>
+// One pass (PASS 0: x1*c1 into y; PASS 1: the cross terms added into y).
+template <int U, int TA, int TB, int PASS, int NPROD>
+int launch_pass(const FirArgs& a, const TcGeom& g0, const __nv_bfloat16* xs,
+                const __nv_bfloat16* Gs, int terms, const DeviceInfo* info, unsigned* err,
+                cudaStream_t st) {
+    constexpr int WB = kKC + 8 * U;
+    TcGeom g = g0;
+    const uint32_t stage = TA * kABytesTerm + TB * kPh * WB * 2;
+    g.stage_bytes = (stage + 1023) / 1024 * 1024;
+    g.tx_bytes = stage;
+    const size_t extra = 1024 + 8 * (2 * 4 + 4) + 16;
+    const int nstage =
+        (int)std::min<int64_t>(4, (info->max_smem_optin - (int64_t)extra) / g.stage_bytes);
+    if (nstage < 2) return set_error(SCIR_ERR_UNSUPPORTED, "tensor-core FIR stage too large");
+    g.nstage = nstage;
+    const size_t smem = (size_t)nstage * g.stage_bytes + extra;
+    CUtensorMap amap;
+    int rc = make_tmap_3d(&amap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, xs, (uint64_t)g.nA,
+                          (uint64_t)a.batch, (uint64_t)terms, (uint64_t)g.nA * 2,
+                          (uint64_t)g.nA * 2 * (uint64_t)a.batch, kKC, kM, 1,
+                          CU_TENSOR_MAP_SWIZZLE_128B);
+    if (rc) return rc;
+    auto kern = fir_tc_kernel<U, TA, TB, PASS, NPROD>;
+    SCIR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t grid = std::min<int64_t>(g.n_tiles, (int64_t)info->sm_count);
+    kern<<<(unsigned)grid, kThreads, smem, st>>>(amap, Gs, g, a.y, a.ld_y, err);
+    SCIR_LAUNCH_CHECK("fir_tc_kernel");
+    return SCIR_OK;
+}
+
+template <int U, int TERMS>
 int launch_tc(const FirArgs& a, cudaStream_t st) {
     const DeviceInfo* info = nullptr;
     int rc = current_device(&info);
@@ -299,21 +333,14 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
     g.batch = a.batch;
     const int64_t ktot = a.k + NCOL - 1;
     g.nchunks = (int)ceil_div(ktot, kKC);
-    constexpr int WB = kKC + 8 * U;
     g.LG = (int64_t)g.nchunks * kKC + 8 * U;
     g.blocks_per_cg = ceil_div(a.n_out, NCOL);
     g.n_tiles = g.blocks_per_cg * ceil_div(a.batch, kM);
-    const uint32_t stage = TERMS * kABytesTerm + TERMS * kPh * WB * 2;
-    g.stage_bytes = (stage + 1023) / 1024 * 1024;
-    g.tx_bytes = stage;
-    const size_t extra = 1024 + 8 * (2 * 4 + 4) + 16;
-    int nstage = (int)std::min<int64_t>(4, (info->max_smem_optin - (int64_t)extra) / g.stage_bytes);
-    if (nstage < 2) return set_error(SCIR_ERR_UNSUPPORTED, "tensor-core FIR stage too large");
-    g.nstage = nstage;
-    const size_t smem = (size_t)nstage * g.stage_bytes + extra;
     g.vec_store = ((reinterpret_cast<uintptr_t>(a.y) & 15) == 0 && (a.ld_y & 3) == 0) ? 1 : 0;
     if (a.n + g.padL + 2 * NCOL + ktot >= (1LL << 31) || ceil_div(a.batch, kM) * kM >= (1LL << 31))
         return set_error(SCIR_ERR_UNSUPPORTED, "tensor-core FIR coordinates exceed 32 bits");
+    unsigned* err = device_error_word();
+    if (!err) return set_error(SCIR_ERR_CUDA, "device error word unavailable");
 
     // split operands into scratch memory
     __nv_bfloat16* xs = nullptr;
@@ -336,26 +363,11 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
         split_taps_kernel<<<gt, 256, 0, st>>>(a.taps, a.k, a.reverse, U, g.LG, TERMS, Gs);
     }
     cudaError_t le = cudaGetLastError();
-    CUtensorMap amap;
-    if (le == cudaSuccess)
-        rc = make_tmap_3d(&amap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, xs, (uint64_t)g.nA,
-                          (uint64_t)a.batch, TERMS, (uint64_t)g.nA * 2,
-                          (uint64_t)g.nA * 2 * (uint64_t)a.batch, kKC, kM, 1,
-                          CU_TENSOR_MAP_SWIZZLE_128B);
-    else
-        rc = set_error(SCIR_ERR_CUDA, "split kernels: %s", cudaGetErrorString(le));
-    unsigned* err = device_error_word();
-    if (rc == SCIR_OK && !err) rc = set_error(SCIR_ERR_CUDA, "device error word unavailable");
+    if (le != cudaSuccess) rc = set_error(SCIR_ERR_CUDA, "split kernels: %s", cudaGetErrorString(le));
+    if (rc == SCIR_OK) rc = launch_pass<U, 1, 1, 0, 1>(a, g, xs, Gs, TERMS, info, err, st);
     if (rc == SCIR_OK) {
-        auto kern = fir_tc_kernel<U, TERMS, NPROD>;
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e == cudaSuccess) {
-            const int64_t grid = std::min<int64_t>(g.n_tiles, (int64_t)info->sm_count);
-            kern<<<(unsigned)grid, kThreads, smem, st>>>(amap, Gs, g, a.y, a.ld_y, err);
-            e = cudaGetLastError();
-        }
-        if (e != cudaSuccess) rc = set_error(SCIR_ERR_CUDA, "fir_tc_kernel: %s", cudaGetErrorString(e));
+        if (TERMS == 2) rc = launch_pass<U, 2, 2, 1, 2>(a, g, xs, Gs, TERMS, info, err, st);
+        else rc = launch_pass<U, 3, 3, 1, 5>(a, g, xs, Gs, TERMS, info, err, st);
     }
     scratch_free(xs, st);
     scratch_free(Gs, st);
@@ -370,8 +382,8 @@ bool fir_tc_supported(const FirArgs& a) {
 
 int launch_fir_tc(const FirArgs& a, int terms, cudaStream_t st) {
     if (a.batch == 0 || a.n_out == 0) return SCIR_OK;
-    if (terms == 2) return launch_tc<32, 2, 3>(a, st);
-    return launch_tc<32, 3, 6>(a, st);
+    if (terms == 2) return launch_tc<64, 2>(a, st);
+    return launch_tc<64, 3>(a, st);
 }
 
 bool poly_tc_supported(const PolyArgs&) { return false; }

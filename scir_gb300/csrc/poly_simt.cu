@@ -50,21 +50,22 @@ struct PolyGeom {
     int64_t off;
     int b00;                      // base of rho = 0 inside a period: off div up
     int IP;                       // periods per work item
-    int nbox;                     // TMA boxes per stage
-    int stage_floats;
+    int nbox;                     // TMA boxes per channel window
+    int win_floats;               // floats per channel window (nbox * kBox)
+    int stage_floats;             // CT windows
     int64_t n_periods, items_per_row, n_items;
     uint8_t unit[kNW][32];        // work unit (pl * G + gl) of each lane; 255 = idle
 };
 
-template <int P, int JWA>
+template <int P, int JWA, int CT>
 __global__ void __launch_bounds__(kThreads, 1)
 poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restrict__ h,
                    int64_t kh, const __grid_constant__ PolyGeom g, float* __restrict__ y,
-                   int64_t ld_y, int64_t n_out, unsigned* __restrict__ err) {
+                   int64_t ld_y, int64_t n_out, int64_t g_batch, unsigned* __restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     float* stages = reinterpret_cast<float*>(smem_raw);
     float* ybuf = stages + kStages * g.stage_floats;
-    uint64_t* full = reinterpret_cast<uint64_t*>(ybuf + kNW * 32 * P);
+    uint64_t* full = reinterpret_cast<uint64_t*>(ybuf + kNW * 32 * P * CT);
     int* done = reinterpret_cast<int*>(full + kStages);  // warps finished with each stage
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -72,13 +73,17 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
     const int shift = (int)(pos_first - (pos_first & ~(int64_t)3));
 
     auto issue = [&](int s, int64_t item) {
-        const int64_t row = item / g.items_per_row;
+        const int64_t row0 = (item / g.items_per_row) * CT;
         const int64_t i0 = (item % g.items_per_row) * g.IP;
         const int64_t pos_a = (i0 * g.down + pos_first) & ~(int64_t)3;
-        float* dst = stages + s * g.stage_floats;
-        mbar_arrive_expect_tx(&full[s], (uint32_t)(g.nbox * kBox * sizeof(float)));
-        for (int b = 0; b < g.nbox; ++b)
-            tma_load_2d(dst + b * kBox, &xmap, &full[s], (int32_t)(pos_a + b * kBox), (int32_t)row);
+        const int rows = (int)min((int64_t)CT, g_batch - row0);
+        mbar_arrive_expect_tx(&full[s], (uint32_t)(rows * g.nbox * kBox * sizeof(float)));
+        for (int r = 0; r < rows; ++r) {
+            float* dst = stages + s * g.stage_floats + r * g.win_floats;
+            for (int b = 0; b < g.nbox; ++b)
+                tma_load_2d(dst + b * kBox, &xmap, &full[s], (int32_t)(pos_a + b * kBox),
+                            (int32_t)(row0 + r));
+        }
     };
 
     if (tid == 0) {
@@ -100,7 +105,7 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
     const int unit = g.unit[warp][lane];
     const bool active = unit < g.G * g.ppw;
     const int gl = active ? unit % g.G : 0, pl = active ? unit / g.G : 0;
-    float* yb = ybuf + warp * 32 * P;
+    float* yb = ybuf + warp * 32 * P * CT;
 
     // --- the thread's tap matrix, fixed for the whole launch
     const int64_t t0 = (int64_t)(gl * P) * g.down + g.off;
@@ -133,39 +138,50 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
             if (lane == 0) atomicOr(err, kErrMbarTimeout);
             break;
         }
-        const int64_t row = item / g.items_per_row;
+        const int64_t row0 = (item / g.items_per_row) * CT;
         const int64_t i0 = (item % g.items_per_row) * g.IP;
         const float* win = stages + s * g.stage_floats;
-        float* __restrict__ yr = y + row * ld_y;
+        const int rows = (int)min((int64_t)CT, g_batch - row0);
+        const int cnt = g.ppw * g.up;
         for (int it = warp; it < iters; it += kNW) {
             const int po = it * g.ppw + pl;  // period offset inside the item
             const int La = (po * g.down + rel0 + shift) & ~3;
-            float acc[P];
+            float acc[CT][P];
 #pragma unroll
-            for (int p = 0; p < P; ++p) acc[p] = 0.0f;
+            for (int r = 0; r < CT; ++r)
+#pragma unroll
+                for (int p = 0; p < P; ++p) acc[r][p] = 0.0f;
             if (active) {
-                const float4* w4 = reinterpret_cast<const float4*>(win + La);
 #pragma unroll
                 for (int j4 = 0; j4 < JWA / 4; ++j4) {
-                    const float4 w = w4[j4];
 #pragma unroll
-                    for (int p = 0; p < P; ++p) {
-                        acc[p] = fmaf(T[p][4 * j4 + 0], w.x, acc[p]);
-                        acc[p] = fmaf(T[p][4 * j4 + 1], w.y, acc[p]);
-                        acc[p] = fmaf(T[p][4 * j4 + 2], w.z, acc[p]);
-                        acc[p] = fmaf(T[p][4 * j4 + 3], w.w, acc[p]);
+                    for (int r = 0; r < CT; ++r) {
+                        // the same tap matrix serves every channel of the item
+                        const float4 w =
+                            reinterpret_cast<const float4*>(win + r * g.win_floats + La)[j4];
+#pragma unroll
+                        for (int p = 0; p < P; ++p) {
+                            acc[r][p] = fmaf(T[p][4 * j4 + 0], w.x, acc[r][p]);
+                            acc[r][p] = fmaf(T[p][4 * j4 + 1], w.y, acc[r][p]);
+                            acc[r][p] = fmaf(T[p][4 * j4 + 2], w.z, acc[r][p]);
+                            acc[r][p] = fmaf(T[p][4 * j4 + 3], w.w, acc[r][p]);
+                        }
                     }
                 }
 #pragma unroll
-                for (int p = 0; p < P; ++p)
-                    if (gl * P + p < g.up) yb[pl * g.up + gl * P + p] = acc[p];
+                for (int r = 0; r < CT; ++r)
+#pragma unroll
+                    for (int p = 0; p < P; ++p)
+                        if (gl * P + p < g.up) yb[r * cnt + pl * g.up + gl * P + p] = acc[r][p];
             }
             __syncwarp();
             const int64_t m0 = (i0 + (int64_t)it * g.ppw) * g.up;
-            const int cnt = g.ppw * g.up;
-            for (int e = lane; e < cnt; e += 32) {
-                const int64_t m = m0 + e;
-                if (m < n_out) yr[m] = yb[e];
+            for (int r = 0; r < rows; ++r) {
+                float* __restrict__ yr = y + (row0 + r) * ld_y;
+                for (int e = lane; e < cnt; e += 32) {
+                    const int64_t m = m0 + e;
+                    if (m < n_out) yr[m] = yb[r * cnt + e];
+                }
             }
             __syncwarp();
         }
@@ -202,13 +218,16 @@ poly_generic_kernel(const float* __restrict__ x, int64_t ld_x, int64_t n,
     y[row * ld_y + m] = acc;
 }
 
-template <int P, int JWA>
+template <int P, int JWA, int CT>
 int launch_stream(const PolyArgs& a, const PolyGeom& g0, cudaStream_t st) {
     const DeviceInfo* info = nullptr;
     int rc = current_device(&info);
     if (rc) return rc;
     PolyGeom g = g0;
-    const size_t smem = sizeof(float) * ((size_t)kStages * g.stage_floats + kNW * 32 * P) +
+    g.stage_floats = CT * g.win_floats;
+    g.items_per_row = ceil_div(g.n_periods, g.IP);
+    g.n_items = g.items_per_row * ceil_div(a.batch, CT);
+    const size_t smem = sizeof(float) * ((size_t)kStages * g.stage_floats + kNW * 32 * P * CT) +
                         kStages * (sizeof(uint64_t) + sizeof(int));
     if ((int)smem > info->max_smem_optin)
         return set_error(SCIR_ERR_UNSUPPORTED, "polyphase stage needs %zu bytes", smem);
@@ -218,10 +237,11 @@ int launch_stream(const PolyArgs& a, const PolyGeom& g0, cudaStream_t st) {
     if (rc) return rc;
     unsigned* err = device_error_word();
     if (!err) return set_error(SCIR_ERR_CUDA, "device error word unavailable");
-    auto kern = poly_stream_kernel<P, JWA>;
+    auto kern = poly_stream_kernel<P, JWA, CT>;
     SCIR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t grid = std::min<int64_t>(g.n_items, (int64_t)info->sm_count);
-    kern<<<(unsigned)grid, kThreads, smem, st>>>(map, a.h, a.kh, g, a.y, a.ld_y, a.n_out, err);
+    kern<<<(unsigned)grid, kThreads, smem, st>>>(map, a.h, a.kh, g, a.y, a.ld_y, a.n_out,
+                                                 a.batch, err);
     SCIR_LAUNCH_CHECK("poly_stream_kernel");
     return SCIR_OK;
 }
@@ -229,13 +249,21 @@ int launch_stream(const PolyArgs& a, const PolyGeom& g0, cudaStream_t st) {
 // Window lengths with a compiled kernel (multiples of 4).
 int jwa_bucket(int jwa) { return jwa <= 12 ? 12 : jwa <= 20 ? 20 : jwa <= 28 ? 28 : 36; }
 
+// Two channels per work item share each thread's tap matrix when there are
+// at least two rows and the doubled accumulators still fit the registers.
+template <int P, int JWA>
+int launch_ct(const PolyArgs& a, const PolyGeom& g, cudaStream_t st) {
+    if (a.batch >= 2 && P * JWA <= 144) return launch_stream<P, JWA, 2>(a, g, st);
+    return launch_stream<P, JWA, 1>(a, g, st);
+}
+
 template <int P>
 int dispatch_jwa(const PolyArgs& a, const PolyGeom& g, int jwa_b, cudaStream_t st) {
     switch (jwa_b) {
-    case 12: return launch_stream<P, 12>(a, g, st);
-    case 20: return launch_stream<P, 20>(a, g, st);
-    case 28: return launch_stream<P, 28>(a, g, st);
-    default: return launch_stream<P, 36>(a, g, st);
+    case 12: return launch_ct<P, 12>(a, g, st);
+    case 20: return launch_ct<P, 20>(a, g, st);
+    case 28: return launch_ct<P, 28>(a, g, st);
+    default: return launch_ct<P, 36>(a, g, st);
     }
 }
 
@@ -331,7 +359,8 @@ int try_stream(const PolyArgs& a, cudaStream_t st) {
     const int64_t need = (int64_t)(g.IP - 1) * a.down + maxrel + 3 + jwa_b + 4;
     if (need > 48 * 1024) return SCIR_ERR_UNSUPPORTED;
     g.nbox = (int)ceil_div(need, kBox);
-    g.stage_floats = g.nbox * kBox;
+    g.win_floats = g.nbox * kBox;
+    g.stage_floats = g.win_floats;
     g.n_periods = ceil_div(a.n_out, a.up);
     g.items_per_row = ceil_div(g.n_periods, g.IP);
     g.n_items = g.items_per_row * a.batch;
