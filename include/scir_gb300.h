@@ -139,6 +139,12 @@ SCIR_API int scir_device_count(int* count);
  * since the last call.  Synchronises with the device.  The reference has no
  * device-side failure reporting (its CUDA path cannot run at all). */
 SCIR_API int scir_device_errors(unsigned* code);
+/* Scratch memory (split operands of the tensor-core FIR, filtfilt edge
+ * extensions) comes from a per-device stream-ordered pool that keeps freed
+ * memory for the next call.  This synchronises the current device and
+ * returns the pool's unused memory.  No reference counterpart (the reference
+ * allocates and frees device buffers on every call). */
+SCIR_API int scir_release_scratch(void);
 
 /* ----------------------------------------------------------------------- */
 /* Batched FIR (device pointers, stream-ordered)                           */

@@ -195,6 +195,12 @@ def device_errors() -> int:
     return int(code.value)
 
 
+def release_scratch() -> None:
+    """Returns the unused memory of the library's scratch pool on the current
+    device (synchronises the device)."""
+    _check(load().scir_release_scratch())
+
+
 def fir_out_len(n: int, k: int, mode: FirMode) -> int:
     v = int(load().scir_fir_out_len(n, k, int(mode)))
     if v < 0:

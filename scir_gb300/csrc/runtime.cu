@@ -97,10 +97,42 @@ int upload_sync(void* dst, const void* src, size_t bytes) {
     return SCIR_OK;
 }
 
+// Scratch memory comes from one stream-ordered pool per device that keeps
+// freed memory (release threshold = unlimited), so repeated calls of the
+// same size reuse it without mapping new pages; scir_release_scratch()
+// returns the pool's unused memory to the device.  The pool is separate from
+// the device's default pool, so the caller's own cudaMallocAsync settings
+// are untouched.
+std::mutex g_pool_mu;
+cudaMemPool_t g_pool[kMaxDevices] = {};
+
+static int scratch_pool(cudaMemPool_t* out) {
+    int dev = 0;
+    SCIR_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return set_error(SCIR_ERR_NO_DEVICE, "bad device %d", dev);
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pool[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        SCIR_CUDA_TRY(cudaMemPoolCreate(&pool, &props));
+        uint64_t keep = ~0ull;
+        SCIR_CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+        g_pool[dev] = pool;
+    }
+    *out = g_pool[dev];
+    return SCIR_OK;
+}
+
 int scratch_alloc(void** p, size_t bytes, cudaStream_t stream) {
     *p = nullptr;
     if (bytes == 0) return SCIR_OK;
-    cudaError_t e = cudaMallocAsync(p, bytes, stream);
+    cudaMemPool_t pool = nullptr;
+    int rc = scratch_pool(&pool);
+    if (rc) return rc;
+    cudaError_t e = cudaMallocFromPoolAsync(p, bytes, pool, stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return set_error(e == cudaErrorMemoryAllocation ? SCIR_ERR_OOM : SCIR_ERR_CUDA,
@@ -248,6 +280,23 @@ SCIR_API int scir_device_errors(unsigned* code) {
     if (!code) return scir::set_error(SCIR_ERR_INVALID_ARG, "code is NULL");
     SCIR_CUDA_TRY(cudaDeviceSynchronize());
     return scir::device_error_take(code);
+}
+
+SCIR_API int scir_release_scratch(void) {
+    scir::clear_error();
+    int dev = 0;
+    SCIR_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= scir::kMaxDevices)
+        return scir::set_error(SCIR_ERR_NO_DEVICE, "bad device %d", dev);
+    cudaMemPool_t pool = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(scir::g_pool_mu);
+        pool = scir::g_pool[dev];
+    }
+    if (!pool) return SCIR_OK;
+    SCIR_CUDA_TRY(cudaDeviceSynchronize());
+    SCIR_CUDA_TRY(cudaMemPoolTrimTo(pool, 0));
+    return SCIR_OK;
 }
 
 SCIR_API int scir_init(int device) {
