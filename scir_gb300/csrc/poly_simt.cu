@@ -53,36 +53,73 @@ struct PolyGeom {
     int nbox;                     // TMA boxes per channel window
     int win_floats;               // floats per channel window (nbox * kBox)
     int stage_floats;             // CT windows
+    int bulk;                     // outputs leave shared memory by bulk copies
+    int bulkin;                   // windows arrive by one bulk copy per row
     int64_t n_periods, items_per_row, n_items;
     uint8_t unit[kNW][32];        // work unit (pl * G + gl) of each lane; 255 = idle
 };
 
 template <int P, int JWA, int CT>
 __global__ void __launch_bounds__(kThreads, 1)
-poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restrict__ h,
+poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restrict__ x,
+                   int64_t ld_x, int64_t n, const float* __restrict__ h,
                    int64_t kh, const __grid_constant__ PolyGeom g, float* __restrict__ y,
                    int64_t ld_y, int64_t n_out, int64_t g_batch, unsigned* __restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     float* stages = reinterpret_cast<float*>(smem_raw);
-    float* ybuf = stages + kStages * g.stage_floats;
-    uint64_t* full = reinterpret_cast<uint64_t*>(ybuf + kNW * 32 * P * CT);
+    float* ybuf = stages + kStages * g.stage_floats;  // two output buffers per warp
+    uint64_t* full = reinterpret_cast<uint64_t*>(ybuf + 2 * kNW * 32 * P * CT);
     int* done = reinterpret_cast<int*>(full + kStages);  // warps finished with each stage
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t pos_first = (int64_t)g.b00 - (g.Q - 1);  // window start of item 0 (i0 = 0)
     const int shift = (int)(pos_first - (pos_first & ~(int64_t)3));
 
-    auto issue = [&](int s, int64_t item) {
+    // Loads item `item` into stage s (called by a whole warp).  Row windows
+    // that start 16-byte aligned come in as one bulk copy per row, clamped
+    // to [0, n); the lanes write the zeros outside the row and the last
+    // n % 4 samples first.  Otherwise lane 0 registers the bytes and the
+    // lanes issue the tensor boxes in parallel (zero fill by TMA).
+    auto issue_warp = [&](int s, int64_t item) {
         const int64_t row0 = (item / g.items_per_row) * CT;
         const int64_t i0 = (item % g.items_per_row) * g.IP;
         const int64_t pos_a = (i0 * g.down + pos_first) & ~(int64_t)3;
         const int rows = (int)min((int64_t)CT, g_batch - row0);
-        mbar_arrive_expect_tx(&full[s], (uint32_t)(rows * g.nbox * kBox * sizeof(float)));
-        for (int r = 0; r < rows; ++r) {
-            float* dst = stages + s * g.stage_floats + r * g.win_floats;
-            for (int b = 0; b < g.nbox; ++b)
-                tma_load_2d(dst + b * kBox, &xmap, &full[s], (int32_t)(pos_a + b * kBox),
-                            (int32_t)(row0 + r));
+        if (g.bulkin) {
+            const int64_t len = g.win_floats;
+            // valid samples [lo, hi) with pos_a <= lo <= hi <= pos_a + len
+            const int64_t lo = min(max(pos_a, (int64_t)0), pos_a + len);
+            const int64_t hi = max(lo, min(pos_a + len, n));
+            const int64_t hi4 = lo + ((hi - lo) & ~(int64_t)3);
+            const int nz_lo = (int)(lo - pos_a), nz_hi = (int)(pos_a + len - hi4);
+            for (int r = 0; r < rows; ++r) {
+                float* w = stages + s * g.stage_floats + r * g.win_floats;
+                const float* xr = x + (row0 + r) * ld_x;
+                for (int e = lane; e < nz_lo; e += 32) w[e] = 0.0f;
+                for (int e = lane; e < nz_hi; e += 32) {
+                    const int64_t src = hi4 + e;
+                    w[src - pos_a] = src < hi ? __ldg(xr + src) : 0.0f;
+                }
+            }
+            __threadfence_block();
+            __syncwarp();
+            if (lane == 0) {
+                const uint32_t bytes = (uint32_t)((hi4 - lo) * (int64_t)sizeof(float));
+                mbar_arrive_expect_tx(&full[s], bytes * (uint32_t)rows);
+                if (bytes > 0)
+                    for (int r = 0; r < rows; ++r)
+                        bulk_load(stages + s * g.stage_floats + r * g.win_floats + (lo - pos_a),
+                                  x + (row0 + r) * ld_x + lo, bytes, &full[s]);
+            }
+            return;
+        }
+        if (lane == 0)
+            mbar_arrive_expect_tx(&full[s], (uint32_t)(rows * g.nbox * kBox * sizeof(float)));
+        __syncwarp();
+        for (int e = lane; e < rows * g.nbox; e += 32) {
+            const int r = e / g.nbox, b = e - r * g.nbox;
+            float* dst = stages + s * g.stage_floats + r * g.win_floats + b * kBox;
+            tma_load_2d(dst, &xmap, &full[s], (int32_t)(pos_a + b * kBox), (int32_t)(row0 + r));
         }
     };
 
@@ -95,17 +132,17 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
         prefetch_tmap(&xmap);
     }
     __syncthreads();
-    if (tid == 0) {
+    if (warp == 0) {
         for (int s = 0; s < kStages; ++s) {
             const int64_t item = blockIdx.x + (int64_t)s * gridDim.x;
-            if (item < g.n_items) issue(s, item);
+            if (item < g.n_items) issue_warp(s, item);
         }
     }
 
     const int unit = g.unit[warp][lane];
     const bool active = unit < g.G * g.ppw;
     const int gl = active ? unit % g.G : 0, pl = active ? unit / g.G : 0;
-    float* yb = ybuf + warp * 32 * P * CT;
+    int ybsel = 0;
 
     // --- the thread's tap matrix, fixed for the whole launch
     const int64_t t0 = (int64_t)(gl * P) * g.down + g.off;
@@ -134,7 +171,8 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
         if (item >= g.n_items) break;
         const int s = (int)(k % kStages);
         const uint32_t parity = (uint32_t)((k / kStages) & 1);
-        if (!mbar_wait(&full[s], parity)) {
+        // warp-uniform outcome: every lane leaves together on a timeout
+        if (!__all_sync(0xffffffffu, mbar_wait(&full[s], parity))) {
             if (lane == 0) atomicOr(err, kErrMbarTimeout);
             break;
         }
@@ -154,49 +192,91 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
             if (active) {
 #pragma unroll
                 for (int j4 = 0; j4 < JWA / 4; ++j4) {
+                    // the same tap matrix serves every channel of the item
+                    float w[CT][4];
 #pragma unroll
                     for (int r = 0; r < CT; ++r) {
-                        // the same tap matrix serves every channel of the item
-                        const float4 w =
+                        const float4 v =
                             reinterpret_cast<const float4*>(win + r * g.win_floats + La)[j4];
-#pragma unroll
-                        for (int p = 0; p < P; ++p) {
-                            acc[r][p] = fmaf(T[p][4 * j4 + 0], w.x, acc[r][p]);
-                            acc[r][p] = fmaf(T[p][4 * j4 + 1], w.y, acc[r][p]);
-                            acc[r][p] = fmaf(T[p][4 * j4 + 2], w.z, acc[r][p]);
-                            acc[r][p] = fmaf(T[p][4 * j4 + 3], w.w, acc[r][p]);
-                        }
+                        w[r][0] = v.x;
+                        w[r][1] = v.y;
+                        w[r][2] = v.z;
+                        w[r][3] = v.w;
                     }
+                    // consecutive FMAs update different accumulators
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+#pragma unroll
+                        for (int r = 0; r < CT; ++r)
+#pragma unroll
+                            for (int p = 0; p < P; ++p)
+                                acc[r][p] = fmaf(T[p][4 * j4 + e], w[r][e], acc[r][p]);
                 }
+            }
+            float* yb = ybuf + (warp * 2 + ybsel) * (32 * P * CT);
+            const int64_t m0 = (i0 + (int64_t)it * g.ppw) * g.up;
+            if (g.bulk) {
+                // the bulk copy issued from this buffer two iterations ago has
+                // finished reading it once at most one group is pending
+                if (lane == 0) bulk_wait_read1();
+                __syncwarp();
+            }
+            if (active) {
 #pragma unroll
                 for (int r = 0; r < CT; ++r)
 #pragma unroll
                     for (int p = 0; p < P; ++p)
                         if (gl * P + p < g.up) yb[r * cnt + pl * g.up + gl * P + p] = acc[r][p];
             }
-            __syncwarp();
-            const int64_t m0 = (i0 + (int64_t)it * g.ppw) * g.up;
-            for (int r = 0; r < rows; ++r) {
-                float* __restrict__ yr = y + (row0 + r) * ld_y;
-                for (int e = lane; e < cnt; e += 32) {
-                    const int64_t m = m0 + e;
-                    if (m < n_out) yr[m] = yb[r * cnt + e];
+            if (g.bulk) {
+                // staged outputs -> global by one bulk copy per channel row
+                fence_proxy_async_smem();
+                __syncwarp();
+                if (lane == 0) {
+                    // outputs [m0, m0 + valid) of each row; periods past the
+                    // row end (valid <= 0) write nothing
+                    const int64_t valid = min((int64_t)cnt, n_out - m0);
+                    if (valid > 0) {
+                        const int64_t v4 = valid & ~(int64_t)3;
+                        for (int r = 0; r < rows; ++r) {
+                            float* __restrict__ yr = y + (row0 + r) * ld_y;
+                            if (v4 > 0)
+                                bulk_store(yr + m0, yb + r * cnt, (uint32_t)(v4 * sizeof(float)));
+                            for (int64_t e = v4; e < valid; ++e) yr[m0 + e] = yb[r * cnt + e];
+                        }
+                    }
+                    bulk_commit();
                 }
+                ybsel ^= 1;
+            } else {
+                __syncwarp();
+                for (int r = 0; r < rows; ++r) {
+                    float* __restrict__ yr = y + (row0 + r) * ld_y;
+                    for (int e = lane; e < cnt; e += 32) {
+                        const int64_t m = m0 + e;
+                        if (m < n_out) yr[m] = yb[r * cnt + e];
+                    }
+                }
+                __syncwarp();
             }
-            __syncwarp();
         }
         // the last warp done with stage s refills it (the fences order every
         // warp's reads of the stage before the refill's writes)
+        int last = 0;
         if (lane == 0) {
             __threadfence_block();
-            if (atomicAdd(&done[s], 1) == kNW - 1) {
+            last = atomicAdd(&done[s], 1) == kNW - 1;
+            if (last) {
                 __threadfence_block();
                 done[s] = 0;
-                const int64_t next = item + (int64_t)kStages * gridDim.x;
-                if (next < g.n_items) issue(s, next);
             }
         }
+        if (__shfl_sync(0xffffffffu, last, 0)) {
+            const int64_t next = item + (int64_t)kStages * gridDim.x;
+            if (next < g.n_items) issue_warp(s, next);
+        }
     }
+    if (g.bulk && lane == 0) bulk_wait_all();
 }
 
 __global__ void __launch_bounds__(256)
@@ -225,9 +305,12 @@ int launch_stream(const PolyArgs& a, const PolyGeom& g0, cudaStream_t st) {
     if (rc) return rc;
     PolyGeom g = g0;
     g.stage_floats = CT * g.win_floats;
+    g.bulk = ((int64_t)g.ppw * g.up % 4 == 0 && (reinterpret_cast<uintptr_t>(a.y) & 15) == 0 &&
+              a.ld_y % 4 == 0) ? 1 : 0;
+    g.bulkin = ((reinterpret_cast<uintptr_t>(a.x) & 15) == 0 && a.ld_x % 4 == 0) ? 1 : 0;
     g.items_per_row = ceil_div(g.n_periods, g.IP);
     g.n_items = g.items_per_row * ceil_div(a.batch, CT);
-    const size_t smem = sizeof(float) * ((size_t)kStages * g.stage_floats + kNW * 32 * P * CT) +
+    const size_t smem = sizeof(float) * ((size_t)kStages * g.stage_floats + 2 * kNW * 32 * P * CT) +
                         kStages * (sizeof(uint64_t) + sizeof(int));
     if ((int)smem > info->max_smem_optin)
         return set_error(SCIR_ERR_UNSUPPORTED, "polyphase stage needs %zu bytes", smem);
@@ -240,8 +323,8 @@ int launch_stream(const PolyArgs& a, const PolyGeom& g0, cudaStream_t st) {
     auto kern = poly_stream_kernel<P, JWA, CT>;
     SCIR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t grid = std::min<int64_t>(g.n_items, (int64_t)info->sm_count);
-    kern<<<(unsigned)grid, kThreads, smem, st>>>(map, a.h, a.kh, g, a.y, a.ld_y, a.n_out,
-                                                 a.batch, err);
+    kern<<<(unsigned)grid, kThreads, smem, st>>>(map, a.x, a.ld_x, a.n, a.h, a.kh, g, a.y, a.ld_y,
+                                                 a.n_out, a.batch, err);
     SCIR_LAUNCH_CHECK("poly_stream_kernel");
     return SCIR_OK;
 }

@@ -97,3 +97,22 @@ def test_resample_host_pipeline(cuda):
     h = S.resample_poly_default_taps(160, 147).astype(np.float32).astype(np.float64)
     ref = O.resample_poly_fast_f64(x[::13].astype(np.float64), 160, 147, h)
     assert normwise_err(y[::13], ref) < TOL_FP32
+
+
+@pytest.mark.parametrize("pad", [0, 3])
+def test_resample_padded_output_rows(cuda, pad):
+    # rows padded to a multiple of 4 floats (16-byte aligned): outputs leave
+    # shared memory by bulk copies, with a row end that is not a multiple of 4;
+    # pad 3 gives an odd row stride and the per-lane store path
+    import torch
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal((5, 20000)).astype(np.float32)
+    n_out = S.resample_poly_out_len(20000, 160, 147)
+    assert n_out % 4 != 0
+    width = (n_out + 3) // 4 * 4 + pad
+    big = torch.full((5, width), 7.0, device=cuda)
+    y = S.resample_poly_f32(_dev(x, cuda), 160, 147, out=big[:, :n_out])
+    h = S.resample_poly_default_taps(160, 147).astype(np.float32).astype(np.float64)
+    ref = O.resample_poly_fast_f64(x.astype(np.float64), 160, 147, h)
+    assert normwise_err(y.cpu().numpy(), ref) < TOL_FP32
+    assert bool((big[:, n_out:] == 7.0).all())  # nothing written past the row end
