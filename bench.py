@@ -529,9 +529,15 @@ class Sos(Workload):
         import scipy.signal as ss
         import scir_gb300 as S
         self.S, self.torch, self.dev = S, torch, dev
-        self.sprec = {S.Precision.AUTO: S.SosPrecision.FP64, S.Precision.FP32: S.SosPrecision.FP32,
-                      S.Precision.REF_EXACT: S.SosPrecision.FP64_EXACT}.get(precision,
-                                                                            S.SosPrecision.FP64)
+        # f32 data: AUTO is the coupled-form FP32 state (<= 1e-5 vs FP64 on this
+        # filter); SOS precision names select a mode directly
+        if isinstance(precision, S.SosPrecision):
+            self.sprec = precision
+        else:
+            self.sprec = {S.Precision.AUTO: S.SosPrecision.FP32_COUPLED,
+                          S.Precision.FP32: S.SosPrecision.FP32,
+                          S.Precision.REF_EXACT: S.SosPrecision.FP64_EXACT}.get(
+                              precision, S.SosPrecision.FP64)
         self.precision = precision
         if channels:
             self.B = channels
@@ -540,7 +546,8 @@ class Sos(Workload):
         self.x = torch.randn((self.B, self.N), device=dev, generator=g)
         self.y = torch.empty_like(self.x)
         self.kernel = "sosfiltfilt_kernel" if self.filtfilt else "sosfilt_kernel"
-        self.bound = "hbm" if self.sprec == S.SosPrecision.FP32 else "fp64"
+        self.bound = "hbm" if self.sprec in (S.SosPrecision.FP32,
+                                             S.SosPrecision.FP32_COUPLED) else "fp64"
 
     def alg_flops(self):
         # 9 flops per section per sample per pass (5 multiplies, 4 adds)
@@ -687,7 +694,12 @@ def run_ours(args):
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
     peaks = load_peaks()
-    prec = S.Precision[args.precision]
+    if args.precision in S.Precision.__members__:
+        prec = S.Precision[args.precision]
+    elif args.workload in ("sosfilt", "sosfiltfilt") and args.precision in S.SosPrecision.__members__:
+        prec = S.SosPrecision[args.precision]
+    else:
+        raise SystemExit(f"unknown precision {args.precision} for {args.workload}")
     W = WORKLOADS[args.workload](torch, dev, prec, args.channels)
     stream = torch.cuda.current_stream(dev)
 
