@@ -60,6 +60,12 @@ struct SosCoef {
 
 // Fills every field of SosCoef from a host [nsec][6] SOS matrix.
 int build_sos_coef(const double* sos, int nsec, bool want_zi, SosCoef* c);
+// FP32-state SOS (FP32, FP32_COUPLED) on f32 data: the cascade split over
+// the warps of a CTA (sos_pipe.cu).
+int launch_sos_pipe(const float* x, int64_t ld_x, int64_t batch, int64_t n, const SosCoef& c,
+                    const double* zi, double* zf, bool filtfilt, int64_t edge, int use_zi,
+                    int precision, float* y, int64_t ld_y, float* tail, cudaStream_t st);
+
 template <typename T>
 int launch_sosfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const SosCoef& c,
                    const double* zi, double* zf, int precision, T* y, int64_t ld_y,

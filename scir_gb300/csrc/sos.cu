@@ -37,85 +37,22 @@
 // and is skipped.
 #include "common.cuh"
 #include "kernels.cuh"
+#include "sos_math.cuh"
+
+#include <type_traits>
 
 namespace scir {
 namespace {
 
 constexpr int kTT = 32;  // samples per tile
 
-template <int PREC>
-struct AccT { using type = double; };
-template <>
-struct AccT<2> { using type = float; };
-template <>
-struct AccT<3> { using type = float; };
-
-// Coefficients are read from the kernel-parameter bank (sc is a __grid_constant__
-// parameter), so they cost no registers; sections past nsec hold b0 = 1.
+// One sample through every section in order.
 template <int NS, int PREC, typename A>
 __device__ __forceinline__ A sos_step(const SosCoef& sc, A (&s1)[NS], A (&s2)[NS], A in) {
     A out = in;
 #pragma unroll
-    for (int s = 0; s < NS; ++s) {
-        const A prev = out;
-        if constexpr (PREC == 0) {
-            const double* c = sc.c[s];
-            out = __dadd_rn(__dmul_rn(c[0], prev), s1[s]);
-            s1[s] = __dadd_rn(__dsub_rn(__dmul_rn(c[1], prev), __dmul_rn(c[3], out)), s2[s]);
-            s2[s] = __dsub_rn(__dmul_rn(c[2], prev), __dmul_rn(c[4], out));
-        } else if constexpr (PREC == 1) {
-            const double* c = sc.c[s];
-            out = fma(c[0], prev, s1[s]);
-            s1[s] = fma(-c[3], out, fma(c[1], prev, s2[s]));
-            s2[s] = fma(-c[4], out, c[2] * prev);
-        } else if constexpr (PREC == 2) {
-            const float* c = sc.cf[s];
-            out = fmaf(c[0], prev, s1[s]);
-            s1[s] = fmaf(-c[3], out, fmaf(c[1], prev, s2[s]));
-            s2[s] = fmaf(-c[4], out, c[2] * prev);
-        } else {
-            if (sc.coupled[s]) {
-                const float* k = sc.cp[s];
-                const float u = s1[s], v = s2[s];
-                out = fmaf(k[2], u, fmaf(k[3], v, k[4] * prev));
-                s1[s] = u + fmaf(k[0], u, fmaf(-k[1], v, prev));
-                s2[s] = v + fmaf(k[1], u, k[0] * v);
-            } else {
-                const float* c = sc.cf[s];
-                out = fmaf(c[0], prev, s1[s]);
-                s1[s] = fmaf(-c[3], out, fmaf(c[1], prev, s2[s]));
-                s2[s] = fmaf(-c[4], out, c[2] * prev);
-            }
-        }
-    }
+    for (int s = 0; s < NS; ++s) out = sos_sec<PREC>(sc, s, s1[s], s2[s], out);
     return out;
-}
-
-// DF2T state (s1, s2) of section s in the kernel's own coordinates.
-template <int PREC, typename A>
-__device__ __forceinline__ void state_in(const SosCoef& sc, int s, double s1, double s2, A& o1,
-                                         A& o2) {
-    if (PREC == 3 && sc.coupled[s]) {
-        const double* m = sc.to_cp[s];
-        o1 = (A)(m[0] * s1 + m[1] * s2);
-        o2 = (A)(m[2] * s1 + m[3] * s2);
-    } else {
-        o1 = (A)s1;
-        o2 = (A)s2;
-    }
-}
-
-template <int PREC, typename A>
-__device__ __forceinline__ void state_out(const SosCoef& sc, int s, A i1, A i2, double& s1,
-                                          double& s2) {
-    if (PREC == 3 && sc.coupled[s]) {
-        const double* m = sc.from_cp[s];
-        s1 = m[0] * (double)i1 + m[1] * (double)i2;
-        s2 = m[2] * (double)i1 + m[3] * (double)i2;
-    } else {
-        s1 = (double)i1;
-        s2 = (double)i2;
-    }
 }
 
 // Loads tile [t0, t0+32) of 32 rows starting at row r0 into registers
@@ -337,6 +274,10 @@ int launch_sosfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const Sos
                    const double* zi, double* zf, int precision, T* y, int64_t ld_y,
                    cudaStream_t st) {
     if (batch == 0) return SCIR_OK;
+    if constexpr (std::is_same<T, float>::value)
+        if (precision == SCIR_SOS_FP32 || precision == SCIR_SOS_FP32_COUPLED)
+            return launch_sos_pipe(x, ld_x, batch, n, c, zi, zf, false, 0, 0, precision, y, ld_y,
+                                   nullptr, st);
     switch (precision) {
     case SCIR_SOS_FP64_EXACT: return dispatch_sosfilt<T, 0>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st);
     case SCIR_SOS_FP64: return dispatch_sosfilt<T, 1>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st);
@@ -352,6 +293,10 @@ int launch_sosfiltfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const
                        int64_t edge, int use_zi, int precision, T* y, int64_t ld_y, T* tail,
                        cudaStream_t st) {
     if (batch == 0 || n == 0) return SCIR_OK;
+    if constexpr (std::is_same<T, float>::value)
+        if (precision == SCIR_SOS_FP32 || precision == SCIR_SOS_FP32_COUPLED)
+            return launch_sos_pipe(x, ld_x, batch, n, c, nullptr, nullptr, true, edge, use_zi,
+                                   precision, y, ld_y, tail, st);
     switch (precision) {
     case SCIR_SOS_FP64_EXACT:
         return dispatch_sosfiltfilt<T, 0>(x, ld_x, batch, n, c, edge, use_zi, y, ld_y, tail, st);

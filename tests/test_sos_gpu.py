@@ -161,3 +161,37 @@ def test_coupled_state_chaining_and_filtfilt(cuda):
     assert np.max(np.abs(zf.cpu().numpy() - ref_zf)) < 1e-4 * np.max(np.abs(ref_zf))
     yff = S.sosfiltfilt_f32(SOS5, xd, precision=P).cpu().numpy()
     assert normwise_err(yff, O.sosfiltfilt_f64(SOS5, x.astype(np.float64))) < TOL
+
+
+# --------------------------------------------------- pipelined FP32 cascade
+# The FP32 modes split the cascade over the warps of a CTA and move tiles of
+# 32 samples through a shared-memory ring (full tiles by a fast path, edge
+# tiles element by element); these lengths cover short signals, tile-boundary
+# remainders, section counts that round up with identity sections and both
+# directions of sosfiltfilt.  A misplaced sample shows as an O(1) error.
+@pytest.mark.parametrize("n", [1, 2, 5, 7, 8, 31, 32, 33, 38, 39, 64, 100, 1000, 20003])
+@pytest.mark.parametrize("order", [1, 4, 16, 18, 40])
+def test_fp32_cascade_lengths(cuda, n, order):
+    sos = ss.butter(order, 0.2, output="sos")
+    rng = np.random.default_rng(n * 100 + order)
+    x = rng.standard_normal((9, n)).astype(np.float32)
+    x64 = x.astype(np.float64)
+    zi = rng.standard_normal((9, sos.shape[0], 2)) * 0.1
+    ref = O.sosfilt_f64(sos, x64)
+    ref_zi = O.sosfilt_f64(sos, x64, zi=zi)
+    for prec, tol in ((S.SosPrecision.FP32_COUPLED, 1e-5), (S.SosPrecision.FP32, 1e-4)):
+        y = S.sosfilt_f32(sos, _dev(x, cuda), precision=prec).cpu().numpy()
+        assert normwise_err(y, ref) < tol, (prec, "sosfilt")
+        y = S.sosfilt_f32(sos, _dev(x, cuda), zi=_dev(zi, cuda), precision=prec).cpu().numpy()
+        assert normwise_err(y, ref_zi) < tol, (prec, "sosfilt zi")
+        padlen = None if n > 3 * (2 * sos.shape[0] + 1) else 0
+        yff = S.sosfiltfilt_f32(sos, _dev(x, cuda), padlen=padlen, precision=prec).cpu().numpy()
+        # a 20-section cascade run forward and backward in FP32 state: measured 1.2e-5 .. 3.9e-5
+        tol_ff = tol * (5 if sos.shape[0] > 16 else 1)
+        assert normwise_err(yff, O.sosfiltfilt_f64(sos, x64, padlen=padlen)) < tol_ff, (prec, "ff")
+        ynp = S.sosfiltfilt_f32(sos, _dev(x, cuda), padtype=S.PadType.NONE, precision=prec).cpu().numpy()
+        ref_np = O.filtfilt_ref_f64(sos, x64)
+        if np.max(np.abs(ref_np)) > 1e-30:  # order 40 at n <= 2: ~1e-46, below FP32's range
+            assert normwise_err(ynp, ref_np) < tol_ff, (prec, "unpadded")
+        else:
+            assert np.all(np.abs(ynp) < 1e-30), (prec, "unpadded, underflow")
