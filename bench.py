@@ -166,6 +166,11 @@ class Workload:
     def samples_per_step(self) -> int:
         raise NotImplementedError
 
+    def autotune(self):
+        """Runs the library's autotuner for this workload's shape (outside the
+        timed region); returns a short description of the choice or None."""
+        return None
+
 
 class Resample(Workload):
     name = "resample_poly_160_147"
@@ -204,6 +209,10 @@ class Resample(Workload):
     def step(self, stream, precision=None):
         self.S.resample_poly_f32(self.x, self.UP, self.DOWN, precision=self.precision if precision is None else precision,
                                  out=self.y, stream=stream)
+
+    def autotune(self):
+        choice, ms = self.S.autotune_resample_poly(self.B, self.N, self.UP, self.DOWN)
+        return f"{choice} ({ms:.3f} ms)"
 
     def max_rel_err(self, precision=None):
         import scipy.signal as ss
@@ -305,6 +314,14 @@ class FirLong(Workload):
                            self.precision if precision is None else precision, out=self.y,
                            stream=stream)
 
+    def autotune(self):
+        P = self.S.Precision
+        if self.precision not in (P.FP32, P.REF_EXACT, P.AUTO):
+            return None
+        choice, ms = self.S.autotune_fir(self.B, self.N, self.K, self.S.FirMode.LFILTER,
+                                         self.precision)
+        return f"{choice} ({ms:.3f} ms)"
+
     def max_rel_err(self, precision=None):
         rows = [0, self.B - 1]
         self.step(None, precision)
@@ -381,6 +398,16 @@ class FirShort(Workload):
 
     def alg_flops(self):
         return 2.0 * self.K * self.B * (2 * self.N)
+
+    def autotune(self):
+        P, M = self.S.Precision, self.S.FirMode
+        if self.precision not in (P.FP32, P.REF_EXACT, P.AUTO):
+            return None
+        out = []
+        for mode in (M.VALID, M.FULL):
+            choice, ms = self.S.autotune_fir(self.B, self.N, self.K, mode, self.precision)
+            out.append(f"{mode.name.lower()}: {choice} ({ms:.3f} ms)")
+        return "; ".join(out)
 
     def step(self, stream, precision=None):
         p = self.precision if precision is None else precision
@@ -468,6 +495,10 @@ class Ragged(Workload):
 
     def step(self, stream, precision=None):
         self.plan.run(self.x, self.taps, self.y, stream=stream)
+
+    def autotune(self):
+        thr, ms = self.plan.autotune(self.x, self.taps, self.y)
+        return f"16 outputs per thread from {thr} taps ({ms:.3f} ms)"
 
     def per_signal_ms(self, stream):
         """The same work as one scir_fir_batched_f32 launch per signal."""
@@ -707,6 +738,7 @@ def run_ours(args):
         if world > 1:
             dist.barrier(device_ids=[local])
 
+    tuned = None if args.no_autotune else W.autotune()
     for _ in range(max(3, args.warmup)):
         W.step(stream)
     torch.cuda.synchronize()
@@ -820,6 +852,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": W.launches_per_step * args.steps,
+        "autotune": tuned,
         "max_rel_err_vs_fp64": err,
         "plain_fp32": plain,
         "per_signal_launches": per_signal,
@@ -838,6 +871,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="resample")
     ap.add_argument("--precision", default="AUTO")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the library autotuner (default dispatch heuristics)")
     ap.add_argument("--channels", type=int, default=None,
                     help="override the channel count (profiling runs on a smaller case)")
     args = ap.parse_args()

@@ -234,6 +234,38 @@ SCIR_API int scir_resample_poly_f32(const float* x, int64_t ld_x, int64_t batch,
                                     int64_t ld_y, void* stream);
 
 /* ----------------------------------------------------------------------- */
+/* Autotuning.  No reference counterpart (the reference has one kernel     */
+/* shape).  Each call times the kernel variants the dispatch can run for    */
+/* one problem shape on synthetic data of that shape (buffers from the      */
+/* library's scratch pool, a private stream, synchronised) and records the  */
+/* fastest for the current device model; later calls with exactly that     */
+/* shape use it.  `choice` receives a short description.                    */
+/* ----------------------------------------------------------------------- */
+
+/* Batched FIR: CUDA-core tiles of 8 or 16 outputs per thread, and for
+ * SCIR_PREC_AUTO also the tensor-core BF16X6 form.  precision must be
+ * REF_EXACT, FP32 or AUTO (the split-bf16 modes have one form). */
+SCIR_API int scir_autotune_fir(int64_t batch, int64_t n, int64_t k, int mode,
+                               int precision, double* best_ms, char* choice,
+                               size_t choice_len);
+/* resample_poly (kh <= 0: the default design's length): outputs per lane
+ * and channels per work item of the streaming kernel. */
+SCIR_API int scir_autotune_resample_poly(int64_t batch, int64_t n, int up,
+                                         int down, int64_t kh, double* best_ms,
+                                         char* choice, size_t choice_len);
+/* Ragged plan: the tap count from which tiles use 16 outputs per thread,
+ * timed on the caller's buffers; the plan's tile list is rebuilt with the
+ * fastest (the stream is synchronised first). */
+SCIR_API int scir_ragged_plan_autotune(scir_ragged_plan* plan, const float* x,
+                                       const float* taps, float* y, void* stream,
+                                       int* v16_min_taps, double* best_ms);
+/* Forgets every recorded choice. */
+SCIR_API int scir_autotune_clear(void);
+/* Writes / merges the recorded choices as text (one line per shape). */
+SCIR_API int scir_autotune_save(const char* path);
+SCIR_API int scir_autotune_load(const char* path);
+
+/* ----------------------------------------------------------------------- */
 /* Second-order sections (device pointers, stream-ordered)                 */
 /* Replaces scir_signal::sosfilt / filtfilt (crates/scir-signal/src/lib.rs:*/
 /* 260-291) over DirectForm2Transposed (crates/scir-iir-filters/src/       */

@@ -195,6 +195,37 @@ def device_errors() -> int:
     return int(code.value)
 
 
+def autotune_fir(batch: int, n: int, k: int, mode: FirMode = FirMode.LFILTER,
+                 precision: Precision = Precision.AUTO):
+    """Times the batched-FIR variants for this shape on the current device and
+    records the fastest; returns (choice, ms per call)."""
+    ms = ctypes.c_double()
+    buf = ctypes.create_string_buffer(64)
+    _check(load().scir_autotune_fir(batch, n, k, int(mode), int(precision), ctypes.byref(ms), buf, 64))
+    return buf.value.decode(), ms.value
+
+
+def autotune_resample_poly(batch: int, n: int, up: int, down: int, kh: int = 0):
+    """Times the polyphase schedules for this shape (kh = 0: the default
+    design) and records the fastest; returns (choice, ms per call)."""
+    ms = ctypes.c_double()
+    buf = ctypes.create_string_buffer(64)
+    _check(load().scir_autotune_resample_poly(batch, n, up, down, kh, ctypes.byref(ms), buf, 64))
+    return buf.value.decode(), ms.value
+
+
+def autotune_save(path: str) -> None:
+    _check(load().scir_autotune_save(path.encode()))
+
+
+def autotune_load(path: str) -> None:
+    _check(load().scir_autotune_load(path.encode()))
+
+
+def autotune_clear() -> None:
+    _check(load().scir_autotune_clear())
+
+
 def release_scratch() -> None:
     """Returns the unused memory of the library's scratch pool on the current
     device (synchronises the device)."""
@@ -419,6 +450,15 @@ class RaggedPlan:
         _check(load().scir_fir_ragged_f32(self._h, x.data_ptr(), taps.data_ptr(), y.data_ptr(),
                                           _stream(stream)))
         return y
+
+    def autotune(self, x, taps, y, stream=None):
+        """Times the tile variants on these buffers and rebuilds the plan with
+        the fastest; returns (16-output tap threshold, ms per launch)."""
+        thr = ctypes.c_int()
+        ms = ctypes.c_double()
+        _check(load().scir_ragged_plan_autotune(self._h, x.data_ptr(), taps.data_ptr(), y.data_ptr(),
+                                                _stream(stream), ctypes.byref(thr), ctypes.byref(ms)))
+        return thr.value, ms.value
 
     def close(self):
         if self._h:

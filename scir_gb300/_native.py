@@ -33,6 +33,15 @@ SIGNATURES = {
     "scir_ragged_plan_stats": (_int, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(ctypes.c_double),
                                       ctypes.POINTER(_i64)]),
     "scir_fir_ragged_f32": (_int, [_vp, _vp, _vp, _vp, _vp]),
+    "scir_ragged_plan_autotune": (_int, [_vp, _vp, _vp, _vp, _vp, ctypes.POINTER(_int),
+                                         ctypes.POINTER(ctypes.c_double)]),
+    "scir_autotune_fir": (_int, [_i64, _i64, _i64, _int, _int, ctypes.POINTER(ctypes.c_double),
+                                 ctypes.c_char_p, _sz]),
+    "scir_autotune_resample_poly": (_int, [_i64, _i64, _int, _int, _i64,
+                                           ctypes.POINTER(ctypes.c_double), ctypes.c_char_p, _sz]),
+    "scir_autotune_clear": (_int, []),
+    "scir_autotune_save": (_int, [ctypes.c_char_p]),
+    "scir_autotune_load": (_int, [ctypes.c_char_p]),
     "scir_upfirdn_out_len": (_i64, [_i64, _i64, _int, _int]),
     "scir_upfirdn_f32": (_int, [_vp, _i64, _i64, _i64, _vp, _i64, _int, _int, _int, _vp, _i64, _vp]),
     "scir_resample_poly_out_len": (_i64, [_i64, _int, _int]),

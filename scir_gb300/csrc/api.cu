@@ -245,6 +245,13 @@ int stage_taps(Stager* s, const void* h, size_t bytes, void** d) {
 }
 
 int fir_dispatch(const FirArgs& a, int precision, cudaStream_t st) {
+    // a shape the autotuner has timed uses its recorded choice
+    const int tuned = (precision == SCIR_PREC_REF_EXACT || precision == SCIR_PREC_FP32 ||
+                       precision == SCIR_PREC_AUTO) ? tune_fir_choice(a, precision) : 0;
+    if (tuned == 1 || tuned == 2)
+        return launch_fir_simt(a, precision == SCIR_PREC_REF_EXACT, st, tuned == 1 ? 8 : 16);
+    if (tuned == 3 && precision == SCIR_PREC_AUTO && fir_tc_supported(a))
+        return launch_fir_tc(a, 3, st);
     switch (precision) {
     case SCIR_PREC_REF_EXACT: return launch_fir_simt(a, true, st);
     case SCIR_PREC_FP32: return launch_fir_simt(a, false, st);
@@ -264,7 +271,10 @@ int poly_dispatch(const PolyArgs& a, int precision, cudaStream_t st) {
     switch (precision) {
     case SCIR_PREC_FP32:
     case SCIR_PREC_REF_EXACT:
-    case SCIR_PREC_AUTO: return launch_poly_simt(a, st);
+    case SCIR_PREC_AUTO: {
+        const int tuned = tune_poly_choice(a);
+        return launch_poly_simt(a, st, tuned / 10, tuned % 10);
+    }
     case SCIR_PREC_BF16X3:
     case SCIR_PREC_BF16X6:
         if (!poly_tc_supported(a))

@@ -45,9 +45,10 @@ int launch_v(const FirArgs& a, cudaStream_t st) {
 
 }  // namespace
 
-int launch_fir_simt(const FirArgs& a, bool exact, cudaStream_t st) {
+int launch_fir_simt(const FirArgs& a, bool exact, cudaStream_t st, int v) {
     if (a.batch == 0 || a.n_out == 0) return SCIR_OK;
-    const bool wide = a.k >= 128;
+    // v = 8 or 16 outputs per thread (autotuned), else by tap count
+    const bool wide = v == 16 ? true : v == 8 ? false : a.k >= 128;
     if (exact) return wide ? launch_v<16, true>(a, st) : launch_v<8, true>(a, st);
     return wide ? launch_v<16, false>(a, st) : launch_v<8, false>(a, st);
 }

@@ -22,7 +22,8 @@ struct FirArgs {
 // Fills reverse / s / n_out from a scir_fir_mode; returns a status.
 int fir_geometry(int64_t n, int64_t k, int mode, int* reverse, int64_t* s, int64_t* n_out);
 
-int launch_fir_simt(const FirArgs& a, bool exact, cudaStream_t st);
+// v: outputs per thread (8 or 16), 0 = by tap count.
+int launch_fir_simt(const FirArgs& a, bool exact, cudaStream_t st, int v = 0);
 // Tensor-core (tcgen05) FIR with split-bf16 operands; terms = 2 (BF16X3) or 3 (BF16X6).
 int launch_fir_tc(const FirArgs& a, int terms, cudaStream_t st);
 bool fir_tc_supported(const FirArgs& a);
@@ -39,7 +40,17 @@ struct PolyArgs {
     float* y;
     int64_t ld_y, n_out;
 };
-int launch_poly_simt(const PolyArgs& a, cudaStream_t st);
+// p_force: outputs per lane (at least the minimum for the rate), ct: channels
+// per work item (1 or 2); 0 = defaults.
+int launch_poly_simt(const PolyArgs& a, cudaStream_t st, int p_force = 0, int ct = 0);
+
+// Autotuning table (tune.cu): the recorded choice for a problem shape on the
+// current device model, or 0 when the shape was never tuned.
+// FIR choice: 1 = CUDA cores, 8 outputs per thread; 2 = CUDA cores, 16;
+// 3 = tensor cores (BF16X6, AUTO precision only).
+int tune_fir_choice(const FirArgs& a, int precision);
+// polyphase choice: P * 10 + CT (0 = untuned).
+int tune_poly_choice(const PolyArgs& a);
 int launch_poly_tc(const PolyArgs& a, int terms, cudaStream_t st);
 bool poly_tc_supported(const PolyArgs& a);
 

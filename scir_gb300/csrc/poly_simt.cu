@@ -335,18 +335,19 @@ int jwa_bucket(int jwa) { return jwa <= 12 ? 12 : jwa <= 20 ? 20 : jwa <= 28 ? 2
 // Two channels per work item share each thread's tap matrix when there are
 // at least two rows and the doubled accumulators still fit the registers.
 template <int P, int JWA>
-int launch_ct(const PolyArgs& a, const PolyGeom& g, cudaStream_t st) {
-    if (a.batch >= 2 && P * JWA <= 144) return launch_stream<P, JWA, 2>(a, g, st);
+int launch_ct(const PolyArgs& a, const PolyGeom& g, int ct, cudaStream_t st) {
+    const bool two = ct == 2 ? a.batch >= 2 : ct == 1 ? false : a.batch >= 2 && P * JWA <= 144;
+    if (two) return launch_stream<P, JWA, 2>(a, g, st);
     return launch_stream<P, JWA, 1>(a, g, st);
 }
 
 template <int P>
-int dispatch_jwa(const PolyArgs& a, const PolyGeom& g, int jwa_b, cudaStream_t st) {
+int dispatch_jwa(const PolyArgs& a, const PolyGeom& g, int jwa_b, int ct, cudaStream_t st) {
     switch (jwa_b) {
-    case 12: return launch_ct<P, 12>(a, g, st);
-    case 20: return launch_ct<P, 20>(a, g, st);
-    case 28: return launch_ct<P, 28>(a, g, st);
-    default: return launch_ct<P, 36>(a, g, st);
+    case 12: return launch_ct<P, 12>(a, g, ct, st);
+    case 20: return launch_ct<P, 20>(a, g, ct, st);
+    case 28: return launch_ct<P, 28>(a, g, ct, st);
+    default: return launch_ct<P, 36>(a, g, ct, st);
     }
 }
 
@@ -412,13 +413,16 @@ void assign_lanes(PolyGeom& g, int /*maxrel*/) {
     }
 }
 
-int try_stream(const PolyArgs& a, cudaStream_t st) {
+int try_stream(const PolyArgs& a, int p_force, int ct, cudaStream_t st) {
     if (a.down > a.up) return SCIR_ERR_UNSUPPORTED;
     if ((reinterpret_cast<uintptr_t>(a.x) & 15) || (a.ld_x & 3)) return SCIR_ERR_UNSUPPORTED;
     if (a.n >= (1LL << 31) - 4096 || a.batch >= (1LL << 31)) return SCIR_ERR_UNSUPPORTED;
     const int64_t Q = ceil_div(a.kh, a.up);
+    // outputs per lane: the fewest that keep a period within 32 lanes, or
+    // more when the autotuner found that faster
     int P = (int)ceil_div(a.up, 32);
     if (P < 1) P = 1;
+    if (p_force > P) P = p_force;
     if (P > 5) return SCIR_ERR_UNSUPPORTED;
     const int JW = (int)Q + P - 1;
     const int jwa = (JW + 3 + 3) / 4 * 4;
@@ -449,10 +453,10 @@ int try_stream(const PolyArgs& a, cudaStream_t st) {
     g.n_items = g.items_per_row * a.batch;
     {
         // the lane assignment depends only on the filter geometry: search once
-        using Key = std::tuple<int, int, int64_t, int>;
+        using Key = std::tuple<int, int, int64_t, int, int>;
         static std::mutex mu;
         static std::map<Key, std::array<uint8_t, kNW * 32>> cache;
-        const Key key{a.up, a.down, a.off, g.Q};
+        const Key key{a.up, a.down, a.off, g.Q, P};
         std::lock_guard<std::mutex> lk(mu);
         auto it = cache.find(key);
         if (it == cache.end()) {
@@ -465,19 +469,19 @@ int try_stream(const PolyArgs& a, cudaStream_t st) {
         }
     }
     switch (P) {
-    case 1: return dispatch_jwa<1>(a, g, jwa_b, st);
-    case 2: return dispatch_jwa<2>(a, g, jwa_b, st);
-    case 3: return dispatch_jwa<3>(a, g, jwa_b, st);
-    case 4: return dispatch_jwa<4>(a, g, jwa_b, st);
-    default: return dispatch_jwa<5>(a, g, jwa_b, st);
+    case 1: return dispatch_jwa<1>(a, g, jwa_b, ct, st);
+    case 2: return dispatch_jwa<2>(a, g, jwa_b, ct, st);
+    case 3: return dispatch_jwa<3>(a, g, jwa_b, ct, st);
+    case 4: return dispatch_jwa<4>(a, g, jwa_b, ct, st);
+    default: return dispatch_jwa<5>(a, g, jwa_b, ct, st);
     }
 }
 
 }  // namespace
 
-int launch_poly_simt(const PolyArgs& a, cudaStream_t st) {
+int launch_poly_simt(const PolyArgs& a, cudaStream_t st, int p_force, int ct) {
     if (a.batch == 0 || a.n_out == 0) return SCIR_OK;
-    int rc = try_stream(a, st);
+    int rc = try_stream(a, p_force, ct, st);
     if (rc != SCIR_ERR_UNSUPPORTED) return rc;
     clear_error();
     const int64_t bpr = ceil_div(a.n_out, 256);

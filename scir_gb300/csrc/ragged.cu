@@ -35,9 +35,11 @@ struct scir_ragged_plan {
     RaggedSig* d_sigs = nullptr;
     RaggedTile* d_tiles = nullptr;
     unsigned long long* d_counter = nullptr;
-    int grid = 0;
+    int grid = 0, per_sm = 0;
     size_t smem = 0;
-    int v16_min_taps = 128;
+    int v16_min_taps = 128;          // tiles of 16 outputs per thread from this tap count
+    std::vector<RaggedSig> h_sigs;   // host copy, for rebuilding the tile list
+    size_t tiles_cap = 0;            // RaggedTile slots allocated at d_tiles
 };
 
 namespace scir {
@@ -74,6 +76,58 @@ ragged_kernel(const RaggedSig* __restrict__ sigs, const RaggedTile* __restrict__
 
 using namespace scir;
 
+namespace scir {
+namespace {
+
+// Cuts every signal into tiles of 256*V outputs (V = 16 from v16_min_taps
+// taps on, else 8), orders them largest-cost first (the shared counter then
+// hands out work in longest-processing-time order), uploads the list and
+// sizes the persistent grid.
+int build_tiles(scir_ragged_plan* p, int v16_min_taps) {
+    std::vector<RaggedTile> tiles;
+    std::vector<double> cost;
+    for (size_t i = 0; i < p->h_sigs.size(); ++i) {
+        const RaggedSig& s = p->h_sigs[i];
+        const int v16 = s.k >= v16_min_taps ? 1 : 0;
+        const int64_t tile = (int64_t)kFirThreads * (v16 ? 16 : 8);
+        for (int64_t o0 = 0; o0 < s.n_out; o0 += tile) {
+            tiles.push_back(RaggedTile{(int32_t)i, v16, o0});
+            cost.push_back((double)std::min<int64_t>(tile, s.n_out - o0) * (double)s.k);
+        }
+    }
+    std::vector<size_t> order(tiles.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t a, size_t b) { return cost[a] > cost[b]; });
+    std::vector<RaggedTile> sorted(tiles.size());
+    for (size_t i = 0; i < order.size(); ++i) sorted[i] = tiles[order[i]];
+    if (sorted.size() > p->tiles_cap || !p->d_tiles) {
+        if (p->d_tiles) cudaFree(p->d_tiles);
+        p->d_tiles = nullptr;
+        p->tiles_cap = 0;
+        cudaError_t e = cudaMalloc(&p->d_tiles, std::max<size_t>(1, sorted.size()) * sizeof(RaggedTile));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(SCIR_ERR_OOM, "ragged tile list allocation failed: %s",
+                             cudaGetErrorString(e));
+        }
+        p->tiles_cap = std::max<size_t>(1, sorted.size());
+    }
+    int rc = upload_sync(p->d_tiles, sorted.data(), sorted.size() * sizeof(RaggedTile));
+    if (rc) return rc;
+    p->ntiles = (int64_t)sorted.size();
+    p->v16_min_taps = v16_min_taps;
+    const DeviceInfo* info = nullptr;
+    rc = current_device(&info);
+    if (rc) return rc;
+    p->grid = (int)std::min<int64_t>((int64_t)p->per_sm * info->sm_count,
+                                     std::max<int64_t>(1, p->ntiles));
+    return SCIR_OK;
+}
+
+}  // namespace
+}  // namespace scir
+
 extern "C" {
 
 SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count, int mode,
@@ -96,8 +150,6 @@ SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count
     p->precision = precision;
     p->count = count;
     std::vector<RaggedSig> sigs((size_t)count);
-    std::vector<RaggedTile> tiles;
-    std::vector<double> cost;
     for (int64_t i = 0; i < count; ++i) {
         const scir_ragged_desc& d = desc[i];
         if (d.n < 0 || d.k < 1 || d.x_off < 0 || d.taps_off < 0 || d.y_off < 0) {
@@ -124,30 +176,12 @@ SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count
         s.pad_ = 0;
         p->samples_in += d.n;
         p->macs += (double)s.n_out * (double)d.k;
-        const int v16 = d.k >= p->v16_min_taps ? 1 : 0;
-        const int64_t tile = (int64_t)kFirThreads * (v16 ? 16 : 8);
-        for (int64_t o0 = 0; o0 < s.n_out; o0 += tile) {
-            tiles.push_back(RaggedTile{(int32_t)i, v16, o0});
-            cost.push_back((double)std::min<int64_t>(tile, s.n_out - o0) * (double)d.k);
-        }
     }
-    // largest tiles first: the shared counter then hands out work in
-    // longest-processing-time order
-    std::vector<size_t> order(tiles.size());
-    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](size_t a, size_t b) { return cost[a] > cost[b]; });
-    std::vector<RaggedTile> sorted(tiles.size());
-    for (size_t i = 0; i < order.size(); ++i) sorted[i] = tiles[order[i]];
-    p->ntiles = (int64_t)sorted.size();
-
     auto fail = [&](int code) {
         scir_ragged_plan_destroy(p);
         return code;
     };
     cudaError_t e = cudaMalloc(&p->d_sigs, std::max<size_t>(1, sigs.size()) * sizeof(RaggedSig));
-    if (e == cudaSuccess)
-        e = cudaMalloc(&p->d_tiles, std::max<size_t>(1, sorted.size()) * sizeof(RaggedTile));
     if (e == cudaSuccess) e = cudaMalloc(&p->d_counter, sizeof(unsigned long long));
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -155,8 +189,8 @@ SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count
         return fail(SCIR_ERR_OOM);
     }
     rc = upload_sync(p->d_sigs, sigs.data(), sigs.size() * sizeof(RaggedSig));
-    if (rc == SCIR_OK) rc = upload_sync(p->d_tiles, sorted.data(), sorted.size() * sizeof(RaggedTile));
     if (rc) return fail(rc);
+    p->h_sigs = std::move(sigs);
     p->smem = fir_tile_smem_bytes(16, kMaxSmemChunk);
     auto kern = precision == SCIR_PREC_REF_EXACT ? ragged_kernel<true> : ragged_kernel<false>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
@@ -168,8 +202,9 @@ SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count
         set_error(SCIR_ERR_CUDA, "ragged kernel occupancy query failed: %s", cudaGetErrorString(e));
         return fail(SCIR_ERR_CUDA);
     }
-    p->grid = (int)std::min<int64_t>((int64_t)per_sm * info->sm_count,
-                                     std::max<int64_t>(1, p->ntiles));
+    p->per_sm = per_sm;
+    rc = build_tiles(p, p->v16_min_taps);
+    if (rc) return fail(rc);
     *plan = p;
     return SCIR_OK;
 }
@@ -211,6 +246,54 @@ SCIR_API int scir_fir_ragged_f32(const scir_ragged_plan* plan, const float* x, c
         ragged_kernel<false><<<plan->grid, kFirThreads, plan->smem, st>>>(
             plan->d_sigs, plan->d_tiles, plan->ntiles, x, taps, y, plan->d_counter);
     SCIR_LAUNCH_CHECK("ragged_kernel");
+    return SCIR_OK;
+}
+
+SCIR_API int scir_ragged_plan_autotune(scir_ragged_plan* plan, const float* x, const float* taps,
+                                       float* y, void* stream, int* v16_min_taps,
+                                       double* best_ms) {
+    clear_error();
+    SCIR_REQUIRE(plan != nullptr, SCIR_ERR_INVALID_ARG, "plan is NULL");
+    if (plan->ntiles == 0) return SCIR_OK;
+    SCIR_REQUIRE(x && taps && y, SCIR_ERR_INVALID_ARG, "NULL buffer");
+    cudaStream_t st = as_stream(stream);
+    // the tile list is rebuilt: nothing queued on the stream may still read it
+    SCIR_CUDA_TRY(cudaStreamSynchronize(st));
+    static const int kCand[] = {32, 64, 128, 256, 512, 1 << 30};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    SCIR_CUDA_TRY(cudaEventCreate(&e0));
+    SCIR_CUDA_TRY(cudaEventCreate(&e1));
+    int best = plan->v16_min_taps, rc = SCIR_OK;
+    float best_t = 0.0f;
+    for (int c : kCand) {
+        rc = build_tiles(plan, c);
+        if (rc) break;
+        rc = scir_fir_ragged_f32(plan, x, taps, y, stream);  // warm-up
+        if (rc) break;
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < 2 && rc == SCIR_OK; ++r) rc = scir_fir_ragged_f32(plan, x, taps, y, stream);
+        cudaEventRecord(e1, st);
+        if (rc) break;
+        cudaError_t ce = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+        if (ce != cudaSuccess) {
+            rc = set_error(SCIR_ERR_CUDA, "ragged autotune timing: %s", cudaGetErrorString(ce));
+            break;
+        }
+        ms *= 0.5f;
+        if (best_t == 0.0f || ms < best_t) {
+            best_t = ms;
+            best = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    rc = build_tiles(plan, best);
+    if (rc) return rc;
+    if (v16_min_taps) *v16_min_taps = best;
+    if (best_ms) *best_ms = best_t;
     return SCIR_OK;
 }
 
