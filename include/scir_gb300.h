@@ -128,8 +128,10 @@ SCIR_API int scir_abi_version(void);
 SCIR_API const char* scir_status_string(int status);
 /* Copies the calling thread's last error message (NUL-terminated). */
 SCIR_API int scir_last_error(char* buf, size_t len);
-/* Initialises per-device state for `device` (kernel attributes, SM count).
- * Optional: every entry point initialises the current device on first use.
+/* Initialises per-device state for `device` (SM count, device error word,
+ * scratch pool) and makes it current.  Optional: every entry point
+ * initialises the current device on first use, but a CUDA-graph capture
+ * needs it done before the capture begins.
  * Replaces cuda_available() / CudaCtx::create_default
  * (crates/scir-gpu/src/lib.rs:596-616). */
 SCIR_API int scir_init(int device);
@@ -232,6 +234,21 @@ SCIR_API int scir_resample_poly_f32(const float* x, int64_t ld_x, int64_t batch,
                                     int64_t n, int up, int down, const float* h,
                                     int64_t kh, int precision, float* y,
                                     int64_t ld_y, void* stream);
+
+/* ----------------------------------------------------------------------- */
+/* CUDA-graph capture of library calls (device layer).  No reference       */
+/* counterpart.  Everything the library enqueues on `stream` between begin  */
+/* and end is recorded and replays with one launch.  Before capturing, call */
+/* scir_init() and make one call of each operation with the same shapes     */
+/* (per-device state and default taps are created on first use).  The       */
+/* capture is thread-local (cudaStreamCaptureModeThreadLocal); the stream   */
+/* must not be the legacy default stream.                                   */
+/* ----------------------------------------------------------------------- */
+typedef struct scir_graph scir_graph;
+SCIR_API int scir_graph_capture_begin(void* stream);
+SCIR_API int scir_graph_capture_end(void* stream, scir_graph** graph);
+SCIR_API int scir_graph_launch(const scir_graph* graph, void* stream);
+SCIR_API int scir_graph_destroy(scir_graph* graph);
 
 /* ----------------------------------------------------------------------- */
 /* Autotuning.  No reference counterpart (the reference has one kernel     */

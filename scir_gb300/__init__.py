@@ -214,6 +214,46 @@ def autotune_resample_poly(batch: int, n: int, up: int, down: int, kh: int = 0):
     return buf.value.decode(), ms.value
 
 
+def init(device: int = 0) -> None:
+    """Creates the library's per-device state for ``device`` and makes it
+    current (needed before a CUDA-graph capture)."""
+    _check(load().scir_init(device))
+
+
+class GraphCapture:
+    """Records the library calls made on ``stream`` inside the ``with`` block
+    into a CUDA graph; ``launch()`` replays them with one launch.  Call
+    ``init()`` and make one call of each operation before capturing."""
+
+    def __init__(self, stream):
+        self.stream = stream
+        self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        _check(load().scir_graph_capture_begin(_stream(self.stream)))
+        return self
+
+    def __exit__(self, exc_type, exc, tb):
+        rc = load().scir_graph_capture_end(_stream(self.stream), ctypes.byref(self._h))
+        if exc_type is None:
+            _check(rc)
+        return False
+
+    def launch(self, stream=None):
+        _check(load().scir_graph_launch(self._h, _stream(self.stream if stream is None else stream)))
+
+    def close(self):
+        if self._h:
+            load().scir_graph_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def autotune_save(path: str) -> None:
     _check(load().scir_autotune_save(path.encode()))
 

@@ -40,6 +40,10 @@ SIGNATURES = {
     "scir_autotune_resample_poly": (_int, [_i64, _i64, _int, _int, _i64,
                                            ctypes.POINTER(ctypes.c_double), ctypes.c_char_p, _sz]),
     "scir_autotune_clear": (_int, []),
+    "scir_graph_capture_begin": (_int, [_vp]),
+    "scir_graph_capture_end": (_int, [_vp, ctypes.POINTER(_vp)]),
+    "scir_graph_launch": (_int, [_vp, _vp]),
+    "scir_graph_destroy": (_int, [_vp]),
     "scir_autotune_save": (_int, [ctypes.c_char_p]),
     "scir_autotune_load": (_int, [ctypes.c_char_p]),
     "scir_upfirdn_out_len": (_i64, [_i64, _i64, _int, _int]),

@@ -33,6 +33,8 @@ int upload_sync(void* dst, const void* src, size_t bytes);
 
 // Stream-ordered scratch allocation (cudaMallocAsync on the caller's stream).
 int scratch_alloc(void** p, size_t bytes, cudaStream_t stream);
+// The library's stream-ordered scratch pool of the current device.
+int scratch_pool(cudaMemPool_t* out);
 void scratch_free(void* p, cudaStream_t stream);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }

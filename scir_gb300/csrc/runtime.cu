@@ -106,7 +106,7 @@ int upload_sync(void* dst, const void* src, size_t bytes) {
 std::mutex g_pool_mu;
 cudaMemPool_t g_pool[kMaxDevices] = {};
 
-static int scratch_pool(cudaMemPool_t* out) {
+int scratch_pool(cudaMemPool_t* out) {
     int dev = 0;
     SCIR_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return set_error(SCIR_ERR_NO_DEVICE, "bad device %d", dev);
@@ -307,7 +307,14 @@ SCIR_API int scir_init(int device) {
         return scir::set_error(SCIR_ERR_INVALID_ARG, "device %d not in [0, %d)", device, count);
     SCIR_CUDA_TRY(cudaSetDevice(device));
     const scir::DeviceInfo* info = nullptr;
-    return scir::current_device(&info);
+    rc = scir::current_device(&info);
+    if (rc) return rc;
+    // state that entry points would otherwise create on first use (and that
+    // must not be created inside a stream capture)
+    if (!scir::device_error_word())
+        return scir::set_error(SCIR_ERR_CUDA, "device error word unavailable");
+    cudaMemPool_t pool = nullptr;
+    return scir::scratch_pool(&pool);
 }
 
 }  // extern "C"

@@ -57,3 +57,46 @@ def test_ragged_exact_and_graph_replay(cuda):
         g.replay()
     torch.cuda.synchronize()
     assert np.array_equal(y2.cpu().numpy(), ref)
+
+
+def test_library_graph_capture_mixed_calls(cuda):
+    """One graph recorded through the C ABI (scir_graph_capture_*) replays a
+    batched FIR, a resample, an SOS cascade and a ragged launch."""
+    import scipy.signal as ss
+    import torch
+    S.init(0)
+    rng = np.random.default_rng(21)
+    x = torch.from_numpy(rng.uniform(-1, 1, (16, 30000)).astype(np.float32)).to(cuda)
+    t = torch.from_numpy(ss.firwin(127, 0.2).astype(np.float32)).to(cuda)
+    sos = ss.butter(8, [0.01, 0.02], btype="bandpass", output="sos")
+    n, k, xr, tr = _ragged_set(22, 12, 20000, 500)
+    plan = S.RaggedPlan(n, k, S.FirMode.LFILTER, S.Precision.FP32)
+    xrd, trd = torch.from_numpy(xr).to(cuda), torch.from_numpy(tr).to(cuda)
+    s = torch.cuda.Stream()
+    outs = {}
+
+    def calls(tag):
+        outs[tag] = [S.fir_batched(x, t, S.FirMode.LFILTER, S.Precision.FP32, out=outs[tag][0], stream=s),
+                     S.resample_poly_f32(x, 160, 147, out=outs[tag][1], stream=s),
+                     S.sosfilt_f32(sos, x, precision=S.SosPrecision.FP32_COUPLED, out=outs[tag][2],
+                                   stream=s),
+                     plan.run(xrd, trd, outs[tag][3], stream=s)]
+
+    n_rs = S.resample_poly_out_len(30000, 160, 147)
+    for tag in ("eager", "graph"):
+        outs[tag] = [torch.zeros_like(x), torch.zeros((16, n_rs), device=cuda), torch.zeros_like(x),
+                     torch.zeros(plan.y_len, device=cuda)]
+    with torch.cuda.stream(s):
+        calls("eager")  # first use creates taps, tensor maps and state outside the capture
+        s.synchronize()
+        with S.GraphCapture(s) as g:
+            calls("graph")
+        for a in outs["graph"]:
+            a.fill_(float("nan"))
+        for _ in range(2):
+            g.launch()
+        s.synchronize()
+    for a, b in zip(outs["eager"], outs["graph"]):
+        assert torch.equal(a, b)
+    g.close()
+    plan.close()
