@@ -236,6 +236,24 @@ SCIR_API int scir_resample_poly_f32(const float* x, int64_t ld_x, int64_t batch,
                                     int64_t ld_y, void* stream);
 
 /* ----------------------------------------------------------------------- */
+/* DeviceArray operations (device pointers, stream-ordered).  Replace the  */
+/* reference's CUDA elementwise kernels add_vec_f32 / add_scalar_f32 /      */
+/* mul_scalar_f32 (crates/scir-gpu/src/lib.rs:629-725) and its CPU-only     */
+/* resize2d_f32 (lib.rs:394-441).  Results equal the reference's CPU values */
+/* bit for bit.                                                             */
+/* ----------------------------------------------------------------------- */
+enum scir_resize_mode { SCIR_RESIZE_NEAREST = 0, SCIR_RESIZE_BILINEAR = 1 };
+SCIR_API int scir_add_vec_f32(const float* a, const float* b, float* out, int64_t n,
+                              void* stream);
+SCIR_API int scir_add_scalar_f32(const float* a, float alpha, float* out, int64_t n,
+                                 void* stream);
+SCIR_API int scir_mul_scalar_f32(const float* a, float alpha, float* out, int64_t n,
+                                 void* stream);
+/* [src_h][src_w] -> [out_h][out_w], half-pixel centres (align_corners = false). */
+SCIR_API int scir_resize2d_f32(const float* src, int64_t src_h, int64_t src_w, float* dst,
+                               int64_t out_h, int64_t out_w, int mode, void* stream);
+
+/* ----------------------------------------------------------------------- */
 /* CUDA-graph capture of library calls (device layer).  No reference       */
 /* counterpart.  Everything the library enqueues on `stream` between begin  */
 /* and end is recorded and replays with one launch.  Before capturing, call */
@@ -281,6 +299,25 @@ SCIR_API int scir_autotune_clear(void);
 /* Writes / merges the recorded choices as text (one line per shape). */
 SCIR_API int scir_autotune_save(const char* path);
 SCIR_API int scir_autotune_load(const char* path);
+
+/* ----------------------------------------------------------------------- */
+/* General IIR (device pointers, stream-ordered).  scipy.signal.lfilter     */
+/* semantics: transposed direct form II over the whole polynomial, b and a  */
+/* divided by a[0], max(na, nb) - 1 <= 32 state values per channel, FP64    */
+/* state and arithmetic.  zi / zf: [batch][max(na, nb) - 1] f64 or NULL.     */
+/* The reference has no general IIR filter (SciPy is the oracle).           */
+/* ----------------------------------------------------------------------- */
+SCIR_API int scir_lfilter_f32(const float* x, int64_t ld_x, int64_t batch,
+                              int64_t n, const double* b, int nb,
+                              const double* a, int na, const double* zi,
+                              double* zf, float* y, int64_t ld_y, void* stream);
+SCIR_API int scir_lfilter_f64(const double* x, int64_t ld_x, int64_t batch,
+                              int64_t n, const double* b, int nb,
+                              const double* a, int na, const double* zi,
+                              double* zf, double* y, int64_t ld_y, void* stream);
+/* scipy.signal.lfilter_zi (host): max(na, nb) - 1 values into zi. */
+SCIR_API int scir_lfilter_zi(const double* b, int nb, const double* a, int na,
+                             double* zi);
 
 /* ----------------------------------------------------------------------- */
 /* Second-order sections (device pointers, stream-ordered)                 */

@@ -58,6 +58,7 @@ def lib():
                 "orc_resample_poly_out_len": (_i64, [_i64, _i64, _i64]),
                 "orc_resample_poly_ref_f64": (_i64, [_vp, _i64, _i64, _i64, _i64, _vp, _i64, _vp]),
                 "orc_resample_poly_fast_f64": (_i64, [_vp, _i64, _i64, _i64, _i64, _vp, _i64, _vp]),
+                "orc_resize2d_f32": (None, [_vp, _i64, _i64, _vp, _i64, _i64, _int]),
             }
             for name, (res, args) in sig.items():
                 fn = getattr(L, name)
@@ -197,3 +198,12 @@ def resample_poly_fast_f64(x, up: int, down: int, h):
     got = lib().orc_resample_poly_fast_f64(_p(x), b, n, up, down, _p(h), h.size, _p(y))
     assert got == nout
     return y
+
+
+def resize2d_f32(img, out_h, out_w, mode):
+    """Reference ``DeviceArray::resize2d_f32`` (mode 0 nearest, 1 bilinear),
+    f32 arithmetic in the reference's order."""
+    img = _c(img, np.float32)
+    out = np.empty((out_h, out_w), np.float32)
+    lib().orc_resize2d_f32(_p(img), img.shape[0], img.shape[1], _p(out), out_h, out_w, int(mode))
+    return out

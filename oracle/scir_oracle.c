@@ -411,3 +411,49 @@ ORC_API int64_t orc_resample_poly_fast_f64(const double* x, int64_t b, int64_t n
     }
     return nout;
 }
+
+/* ------------------------------------------------------------------------
+ * DeviceArray::resize2d_f32 (crates/scir-gpu/src/lib.rs:394-441): half-pixel
+ * centre mapping, mode 0 nearest (round half away from zero, clamped), mode 1
+ * bilinear; f32 arithmetic in the reference's order (compiled without FMA
+ * contraction).
+ * ---------------------------------------------------------------------- */
+void orc_resize2d_f32(const float* src, int64_t src_h, int64_t src_w, float* dst, int64_t out_h,
+                      int64_t out_w, int mode) {
+    const float scale_x = (float)src_w / (float)out_w;
+    const float scale_y = (float)src_h / (float)out_h;
+    for (int64_t dy = 0; dy < out_h; ++dy) {
+        for (int64_t dx = 0; dx < out_w; ++dx) {
+            float sx = ((float)dx + 0.5f) * scale_x - 0.5f;
+            float sy = ((float)dy + 0.5f) * scale_y - 0.5f;
+            if (sx < 0.0f) sx = 0.0f;
+            if (sy < 0.0f) sy = 0.0f;
+            float v;
+            if (mode == 0) {
+                float fx = roundf(sx), fy = roundf(sy);
+                const float mx = (float)src_w - 1.0f, my = (float)src_h - 1.0f;
+                fx = fx < 0.0f ? 0.0f : (fx > mx ? mx : fx);
+                fy = fy < 0.0f ? 0.0f : (fy > my ? my : fy);
+                v = src[(int64_t)fy * src_w + (int64_t)fx];
+            } else {
+                const float mx = (float)src_w - 1.0f, my = (float)src_h - 1.0f;
+                float x0 = floorf(sx), y0 = floorf(sy);
+                x0 = x0 < 0.0f ? 0.0f : (x0 > mx ? mx : x0);
+                y0 = y0 < 0.0f ? 0.0f : (y0 > my ? my : y0);
+                const float x1 = (x0 + 1.0f) < mx ? (x0 + 1.0f) : mx;
+                const float y1 = (y0 + 1.0f) < my ? (y0 + 1.0f) : my;
+                float fx = sx - x0, fy = sy - y0;
+                fx = fx < 0.0f ? 0.0f : (fx > 1.0f ? 1.0f : fx);
+                fy = fy < 0.0f ? 0.0f : (fy > 1.0f ? 1.0f : fy);
+                const int64_t ix0 = (int64_t)x0, iy0 = (int64_t)y0, ix1 = (int64_t)x1,
+                              iy1 = (int64_t)y1;
+                const float v00 = src[iy0 * src_w + ix0], v10 = src[iy0 * src_w + ix1];
+                const float v01 = src[iy1 * src_w + ix0], v11 = src[iy1 * src_w + ix1];
+                const float top = v00 + (v10 - v00) * fx;
+                const float bot = v01 + (v11 - v01) * fx;
+                v = top + (bot - top) * fy;
+            }
+            dst[dy * out_w + dx] = v;
+        }
+    }
+}

@@ -220,6 +220,58 @@ def init(device: int = 0) -> None:
     _check(load().scir_init(device))
 
 
+class ResizeMode(enum.IntEnum):
+    NEAREST = 0
+    BILINEAR = 1
+
+
+def _f32_flat(t, name):
+    torch = _torch()
+    if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float32:
+        raise GpuError(ERR_INVALID_ARG, f"{name} must be a float32 CUDA tensor")
+    if not t.is_contiguous():
+        raise GpuError(ERR_INVALID_ARG, f"{name} must be contiguous")
+    return t
+
+
+def add_vec(a, b, out=None, stream=None):
+    """DeviceArray::add_auto on the GPU: out = a + b (same shape, float32)."""
+    a, b = _f32_flat(a, "a"), _f32_flat(b, "b")
+    if a.shape != b.shape:
+        raise GpuError(ERR_SHAPE, "shape mismatch")
+    out = _torch().empty_like(a) if out is None else _f32_flat(out, "out")
+    _check(load().scir_add_vec_f32(a.data_ptr(), b.data_ptr(), out.data_ptr(), a.numel(),
+                                   _stream(stream)))
+    return out
+
+
+def add_scalar(a, alpha: float, out=None, stream=None):
+    a = _f32_flat(a, "a")
+    out = _torch().empty_like(a) if out is None else _f32_flat(out, "out")
+    _check(load().scir_add_scalar_f32(a.data_ptr(), float(alpha), out.data_ptr(), a.numel(),
+                                      _stream(stream)))
+    return out
+
+
+def mul_scalar(a, alpha: float, out=None, stream=None):
+    a = _f32_flat(a, "a")
+    out = _torch().empty_like(a) if out is None else _f32_flat(out, "out")
+    _check(load().scir_mul_scalar_f32(a.data_ptr(), float(alpha), out.data_ptr(), a.numel(),
+                                      _stream(stream)))
+    return out
+
+
+def resize2d(img, out_h: int, out_w: int, mode: ResizeMode = ResizeMode.BILINEAR, stream=None):
+    """DeviceArray::resize2d_f32 on a [height, width] float32 CUDA tensor."""
+    img = _f32_flat(img, "img")
+    if img.dim() != 2:
+        raise GpuError(ERR_SHAPE, "resize2d needs a 2-D [height, width] tensor")
+    out = _torch().empty((out_h, out_w), device=img.device, dtype=img.dtype)
+    _check(load().scir_resize2d_f32(img.data_ptr(), img.shape[0], img.shape[1], out.data_ptr(),
+                                    out_h, out_w, int(mode), _stream(stream)))
+    return out
+
+
 class GraphCapture:
     """Records the library calls made on ``stream`` inside the ``with`` block
     into a CUDA graph; ``launch()`` replays them with one launch.  Call
@@ -303,6 +355,15 @@ def sosfilt_zi(sos) -> np.ndarray:
     zi = np.empty((sos.shape[0], 2), np.float64)
     _check(load().scir_sosfilt_zi(_ptr(sos), sos.shape[0], _ptr(zi)))
     return zi
+
+
+def lfilter_zi(b, a) -> np.ndarray:
+    """scipy.signal.lfilter_zi (max(len(a), len(b)) - 1 values)."""
+    b = np.ascontiguousarray(np.atleast_1d(b), np.float64)
+    a = np.ascontiguousarray(np.atleast_1d(a), np.float64)
+    zi = np.empty(max(max(b.size, a.size) - 1, 1), np.float64)
+    _check(load().scir_lfilter_zi(_ptr(b), b.size, _ptr(a), a.size, _ptr(zi)))
+    return zi[:max(b.size, a.size) - 1]
 
 
 def sosfiltfilt_default_padlen(sos) -> int:
@@ -405,6 +466,32 @@ def _sosfilt_dev(fn, dtype, sos, x, zi, return_zf, precision, out, stream):
     _check(fn(x2.data_ptr(), ldx, x2.shape[0], x2.shape[1], _ptr(sos), nsec, zip_,
               zf.data_ptr() if zf is not None else None, int(precision), y2.data_ptr(), ldy,
               _stream(stream)))
+    return (out, zf) if return_zf else out
+
+
+def lfilter(b, a, x, zi=None, return_zf: bool = False, out=None, stream=None):
+    """scipy.signal.lfilter(b, a, x, axis=-1, zi) along the rows of CUDA tensor
+    x (float32 or float64); zi / zf are (batch, max(len(a), len(b)) - 1)
+    float64."""
+    torch = _torch()
+    b = np.ascontiguousarray(np.atleast_1d(b), np.float64)
+    a = np.ascontiguousarray(np.atleast_1d(a), np.float64)
+    dtype = x.dtype
+    if dtype not in (torch.float32, torch.float64):
+        raise GpuError(ERR_INVALID_ARG, "x must be float32 or float64")
+    x2, ldx = _rows(x, dtype, "x")
+    if out is None:
+        out = torch.empty_like(x2)
+    y2, ldy = _rows(out, dtype, "out")
+    ns = max(a.size, b.size) - 1
+    zip_ = None
+    if zi is not None:
+        zi = zi.to(device=x.device, dtype=torch.float64).expand(x2.shape[0], ns).contiguous()
+        zip_ = zi.data_ptr()
+    zf = torch.empty((x2.shape[0], ns), device=x.device, dtype=torch.float64) if return_zf else None
+    fn = load().scir_lfilter_f32 if dtype == torch.float32 else load().scir_lfilter_f64
+    _check(fn(x2.data_ptr(), ldx, x2.shape[0], x2.shape[1], _ptr(b), b.size, _ptr(a), a.size, zip_,
+              zf.data_ptr() if zf is not None else None, y2.data_ptr(), ldy, _stream(stream)))
     return (out, zf) if return_zf else out
 
 

@@ -40,6 +40,10 @@ SIGNATURES = {
     "scir_autotune_resample_poly": (_int, [_i64, _i64, _int, _int, _i64,
                                            ctypes.POINTER(ctypes.c_double), ctypes.c_char_p, _sz]),
     "scir_autotune_clear": (_int, []),
+    "scir_add_vec_f32": (_int, [_vp, _vp, _vp, _i64, _vp]),
+    "scir_add_scalar_f32": (_int, [_vp, ctypes.c_float, _vp, _i64, _vp]),
+    "scir_mul_scalar_f32": (_int, [_vp, ctypes.c_float, _vp, _i64, _vp]),
+    "scir_resize2d_f32": (_int, [_vp, _i64, _i64, _vp, _i64, _i64, _int, _vp]),
     "scir_graph_capture_begin": (_int, [_vp]),
     "scir_graph_capture_end": (_int, [_vp, ctypes.POINTER(_vp)]),
     "scir_graph_launch": (_int, [_vp, _vp]),
@@ -55,6 +59,11 @@ SIGNATURES = {
     "scir_sosfilt_f32": (_int, [_vp, _i64, _i64, _i64, _vp, _int, _vp, _vp, _int, _vp, _i64, _vp]),
     "scir_sosfilt_f64": (_int, [_vp, _i64, _i64, _i64, _vp, _int, _vp, _vp, _int, _vp, _i64, _vp]),
     "scir_sosfilt_zi": (_int, [_vp, _int, _vp]),
+    "scir_lfilter_f32": (_int, [_vp, _i64, _i64, _i64, _vp, _int, _vp, _int, _vp, _vp, _vp, _i64,
+                                _vp]),
+    "scir_lfilter_f64": (_int, [_vp, _i64, _i64, _i64, _vp, _int, _vp, _int, _vp, _vp, _vp, _i64,
+                                _vp]),
+    "scir_lfilter_zi": (_int, [_vp, _int, _vp, _int, _vp]),
     "scir_sosfiltfilt_default_padlen": (_i64, [_vp, _int]),
     "scir_sosfiltfilt_f32": (_int, [_vp, _i64, _i64, _i64, _vp, _int, _int, _i64, _int, _vp, _i64,
                                     _vp]),

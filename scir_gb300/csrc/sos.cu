@@ -44,7 +44,6 @@
 namespace scir {
 namespace {
 
-constexpr int kTT = 32;  // samples per tile
 
 // One sample through every section in order.
 template <int NS, int PREC, typename A>
@@ -53,32 +52,6 @@ __device__ __forceinline__ A sos_step(const SosCoef& sc, A (&s1)[NS], A (&s2)[NS
 #pragma unroll
     for (int s = 0; s < NS; ++s) out = sos_sec<PREC>(sc, s, s1[s], s2[s], out);
     return out;
-}
-
-// Loads tile [t0, t0+32) of 32 rows starting at row r0 into registers
-// (lane = time); rows past `batch` and samples past n read as zero.
-template <typename T>
-__device__ __forceinline__ void tile_fetch(T (&r)[kTT], const T* __restrict__ x, int64_t ld,
-                                           int64_t r0, int64_t batch, int64_t n, int64_t t0,
-                                           int lane) {
-    const int64_t t = t0 + lane;
-#pragma unroll
-    for (int i = 0; i < kTT; ++i) {
-        const int64_t row = r0 + i;
-        r[i] = (row < batch && t < n && t >= 0) ? x[row * ld + t] : T(0);
-    }
-}
-
-template <typename T>
-__device__ __forceinline__ void tile_store(T (*s)[kTT + 1], T* __restrict__ y, int64_t ld,
-                                           int64_t r0, int64_t batch, int64_t n, int64_t t0,
-                                           int lane) {
-    const int64_t t = t0 + lane;
-#pragma unroll 4
-    for (int i = 0; i < kTT; ++i) {
-        const int64_t row = r0 + i;
-        if (row < batch && t < n) y[row * ld + t] = s[i][lane];
-    }
 }
 
 template <typename T, int NS, int PREC>

@@ -1,6 +1,7 @@
-// Second-order-section arithmetic shared by the SOS kernels: one section
-// update in each state precision, and the exchange of section states with the
-// DF2T coordinates of the API (zi / zf).
+// Arithmetic shared by the SOS and IIR kernels: one section update in each
+// state precision, the exchange of section states with the DF2T coordinates
+// of the API (zi / zf), and the 32 x 32 row tiles of the one-thread-per-
+// channel kernels.
 //
 // The recursion is the reference's Direct Form II transposed cascade
 // (crates/scir-iir-filters/src/filter.rs:50-61):
@@ -85,6 +86,37 @@ __device__ __forceinline__ void state_out(const SosCoef& sc, int s, A i1, A i2, 
     } else {
         s1 = (double)i1;
         s2 = (double)i2;
+    }
+}
+
+// Row tiles of 32 channels x 32 samples for one-thread-per-channel
+// recursions: a warp loads a tile row by row (coalesced) into registers,
+// transposes it through a [32][33] shared tile, and stores it back row by row.
+constexpr int kTT = 32;  // samples per tile
+
+// Loads tile [t0, t0+32) of 32 rows starting at row r0 into registers
+// (lane = time); rows past `batch` and samples past n read as zero.
+template <typename T>
+__device__ __forceinline__ void tile_fetch(T (&r)[kTT], const T* __restrict__ x, int64_t ld,
+                                           int64_t r0, int64_t batch, int64_t n, int64_t t0,
+                                           int lane) {
+    const int64_t t = t0 + lane;
+#pragma unroll
+    for (int i = 0; i < kTT; ++i) {
+        const int64_t row = r0 + i;
+        r[i] = (row < batch && t < n && t >= 0) ? x[row * ld + t] : T(0);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void tile_store(T (*s)[kTT + 1], T* __restrict__ y, int64_t ld,
+                                           int64_t r0, int64_t batch, int64_t n, int64_t t0,
+                                           int lane) {
+    const int64_t t = t0 + lane;
+#pragma unroll 4
+    for (int i = 0; i < kTT; ++i) {
+        const int64_t row = r0 + i;
+        if (row < batch && t < n) y[row * ld + t] = s[i][lane];
     }
 }
 

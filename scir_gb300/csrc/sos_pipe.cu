@@ -42,7 +42,7 @@
 namespace scir {
 namespace {
 
-constexpr int kTT = 32;     // channels per CTA = samples per tile
+// kTT (32, from sos_math.cuh): channels per CTA = samples per tile
 constexpr int kRing = 8;    // tile slots
 constexpr int kLd = kTT + 1;
 
