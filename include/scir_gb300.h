@@ -284,7 +284,7 @@ SCIR_API int scir_autotune_fir(int64_t batch, int64_t n, int64_t k, int mode,
                                int precision, double* best_ms, char* choice,
                                size_t choice_len);
 /* resample_poly (kh <= 0: the default design's length): outputs per lane
- * and channels per work item of the streaming kernel. */
+ * and channels per work item (1, 2 or 4) of the streaming kernel. */
 SCIR_API int scir_autotune_resample_poly(int64_t batch, int64_t n, int up,
                                          int down, int64_t kh, double* best_ms,
                                          char* choice, size_t choice_len);

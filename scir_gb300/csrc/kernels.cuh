@@ -41,7 +41,7 @@ struct PolyArgs {
     int64_t ld_y, n_out;
 };
 // p_force: outputs per lane (at least the minimum for the rate), ct: channels
-// per work item (1 or 2); 0 = defaults.
+// per work item (1, 2 or 4); 0 = defaults.
 int launch_poly_simt(const PolyArgs& a, cudaStream_t st, int p_force = 0, int ct = 0);
 
 // Autotuning table (tune.cu): the recorded choice for a problem shape on the

@@ -7,7 +7,8 @@
 //     only other form that holds 1e-5).  The default without tuning is 16
 //     from 128 taps on and the tensor cores from 512 taps on.
 //   resample_poly / upfirdn: outputs per lane P (from the minimum that keeps
-//     a period within one warp up to 5) and channels per work item (1 or 2).
+//     a period within one warp up to 5) and channels per work item (1, 2 or
+//     4; four use items of 16 periods).
 //   ragged FIR: the tap count from which tiles use 16 outputs per thread
 //     (scir_ragged_plan_autotune, in ragged.cu).
 //
@@ -272,7 +273,7 @@ SCIR_API int scir_autotune_resample_poly(int64_t batch, int64_t n, int up, int d
     float best_t = 0.0f;
     const int pmax = std::min(5, std::max(pmin, upr));  // more outputs per lane than up idle lanes
     for (int P = pmin; P <= pmax && !rc; ++P) {
-        for (int ct = 1; ct <= (batch >= 2 ? 2 : 1) && !rc; ++ct) {
+        for (int ct = 1; ct <= (batch >= 4 ? 4 : batch >= 2 ? 2 : 1) && !rc; ct *= 2) {
             float t = 0.0f;
             rc = time_calls([&]() -> int { return launch_poly_simt(a, st, P, ct); }, st, 3, &t);
             if (!rc && (best == 0 || t < best_t)) {
@@ -356,8 +357,8 @@ SCIR_API int scir_autotune_load(const char* path) {
             fir[FirKey{model, b, n, k, no, rev, s, prec}] = ch;
         } else if (!strcmp(kind, "poly") &&
                    sscanf(line, "poly %255s %lld %lld %lld %d %d %lld %d", model, &b, &n, &kh, &up,
-                          &dn, &off, &ch) == 8 && ch / 10 >= 1 && ch / 10 <= 5 && ch % 10 >= 1 &&
-                   ch % 10 <= 2) {
+                          &dn, &off, &ch) == 8 && ch / 10 >= 1 && ch / 10 <= 5 &&
+                   (ch % 10 == 1 || ch % 10 == 2 || ch % 10 == 4)) {
             poly[PolyKey{model, b, n, kh, up, dn, off}] = ch;
         } else {
             bad = lineno + 1;

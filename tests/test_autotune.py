@@ -114,3 +114,25 @@ def test_autotuned_ragged_plan(cuda):
                           for i in range(len(n))])
     assert np.array_equal(y.cpu().numpy(), ref)
     plan.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ct", [1, 2, 4])
+def test_polyphase_schedules_via_table(cuda, tmp_path, ct):
+    """Every channels-per-item schedule, forced through a loaded table, gives
+    the oracle's result (6 channels: the last item of 4 holds 2 rows)."""
+    S.autotune_clear()
+    S.autotune_resample_poly(2, 1000, 160, 147)  # any tuned entry reveals the model tag
+    path = tmp_path / "t.txt"
+    S.autotune_save(str(path))
+    model = path.read_text().splitlines()[1].split()[1]
+    n = 20000
+    path.write_text(f"scir-autotune 1\npoly {model} 6 {n} 3201 160 147 1600 {50 + ct}\n")
+    S.autotune_clear()
+    S.autotune_load(str(path))
+    rng = np.random.default_rng(ct)
+    x = rng.standard_normal((6, n)).astype(np.float32)
+    y = S.resample_poly_f32(_dev(x, cuda), 160, 147).cpu().numpy()
+    h = S.resample_poly_default_taps(160, 147).astype(np.float32).astype(np.float64)
+    assert normwise_err(y, O.resample_poly_fast_f64(x.astype(np.float64), 160, 147, h)) < 1e-5
+    S.autotune_clear()
