@@ -320,6 +320,52 @@ SCIR_API int scir_lfilter_zi(const double* b, int nb, const double* a, int na,
                              double* zi);
 
 /* ----------------------------------------------------------------------- */
+/* IIR design (host, FP64, no device).  Replaces the reference's butter /   */
+/* cheby1 / bessel_with_norm -> iirfilter (crates/scir-iir-filters/src/     */
+/* filter_design.rs:128-314) and zpk2sos (crates/scir-iir-filters/src/      */
+/* sos.rs:154-357), SciPy semantics.  wn holds one edge (low/high-pass) or  */
+/* two increasing edges (band-pass/stop) in the units of fs; fs <= 0 means  */
+/* the edges are already normalised to Nyquist = 1.  rp (dB, > 0) is read   */
+/* for Chebyshev I only.  Bessel orders 1..25 (the reference's range),      */
+/* others 0..256.  Complex values are interleaved (re, im) pairs.           */
+/* ----------------------------------------------------------------------- */
+enum scir_iir_family {
+    SCIR_IIR_BUTTER = 0,
+    SCIR_IIR_CHEBY1 = 1,
+    SCIR_IIR_BESSEL_PHASE = 2, /* BesselNorm::Phase (SciPy's default) */
+    SCIR_IIR_BESSEL_DELAY = 3, /* BesselNorm::Delay                   */
+    SCIR_IIR_BESSEL_MAG = 4    /* BesselNorm::Mag                     */
+};
+enum scir_band_type {
+    SCIR_BAND_LOWPASS = 0,
+    SCIR_BAND_HIGHPASS = 1,
+    SCIR_BAND_BANDPASS = 2,
+    SCIR_BAND_BANDSTOP = 3
+};
+/* SosPairing (crates/scir-iir-filters/src/sos.rs:22-35). */
+enum scir_sos_pairing {
+    SCIR_PAIR_NEAREST = 0,
+    SCIR_PAIR_KEEP_ODD = 1,
+    SCIR_PAIR_MINIMAL = 2
+};
+/* Digital zeros, poles and gain.  *nz, *np and *k are always written; z
+ * and p ([cap][2] each) only when both are non-NULL (cap >= *nz, *np). */
+SCIR_API int scir_iirfilter_zpk(int order, int family, int btype,
+                                const double* wn, double rp, double fs,
+                                double* z, double* p, int cap, int* nz,
+                                int* np, double* k);
+/* Sections [nsec][6] (b0 b1 b2 a0 a1 a2) of a zpk system; *nsec is always
+ * written, sos only when non-NULL (cap >= *nsec). */
+SCIR_API int scir_zpk2sos(const double* z, int nz, const double* p, int np,
+                          double k, int pairing, double* sos, int cap,
+                          int* nsec);
+/* iirfilter(..., output='sos'): scir_iirfilter_zpk then scir_zpk2sos with
+ * nearest pairing; ceil(order / 2) sections (order for band filters). */
+SCIR_API int scir_iirfilter_sos(int order, int family, int btype,
+                                const double* wn, double rp, double fs,
+                                double* sos, int cap, int* nsec);
+
+/* ----------------------------------------------------------------------- */
 /* Second-order sections (device pointers, stream-ordered)                 */
 /* Replaces scir_signal::sosfilt / filtfilt (crates/scir-signal/src/lib.rs:*/
 /* 260-291) over DirectForm2Transposed (crates/scir-iir-filters/src/       */

@@ -29,7 +29,8 @@ __all__ = [
     "resample_poly", "resample_poly_host", "fir_batched", "fir_out_len", "upfirdn",
     "upfirdn_out_len", "resample_poly_f32", "resample_poly_out_len", "resample_poly_default_taps",
     "sosfilt_f32", "sosfilt_f64", "sosfiltfilt_f32", "sosfiltfilt_f64", "sosfilt_zi",
-    "sosfiltfilt_default_padlen", "RaggedPlan", "load", "device_errors",
+    "sosfiltfilt_default_padlen", "RaggedPlan", "load", "device_errors", "FilterFamily", "BandType",
+    "SosPairing", "iirfilter", "butter", "cheby1", "bessel", "zpk2sos",
 ]
 
 OK, ERR_INVALID_ARG, ERR_SHAPE, ERR_ALIGN, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED, \
@@ -369,6 +370,115 @@ def lfilter_zi(b, a) -> np.ndarray:
 def sosfiltfilt_default_padlen(sos) -> int:
     sos = _sos_array(sos)
     return int(load().scir_sosfiltfilt_default_padlen(_ptr(sos), sos.shape[0]))
+
+
+# --------------------------------------------------------------------------- IIR design (host)
+
+class FilterFamily(enum.IntEnum):
+    """scir_iir_family: the prototype (and Bessel normalisation)."""
+    BUTTER = 0
+    CHEBY1 = 1
+    BESSEL_PHASE = 2
+    BESSEL_DELAY = 3
+    BESSEL_MAG = 4
+
+
+class BandType(enum.IntEnum):
+    LOWPASS = 0
+    HIGHPASS = 1
+    BANDPASS = 2
+    BANDSTOP = 3
+
+
+class SosPairing(enum.IntEnum):
+    """SosPairing (crates/scir-iir-filters/src/sos.rs:22-35)."""
+    NEAREST = 0
+    KEEP_ODD = 1
+    MINIMAL = 2
+
+
+_BTYPE_NAMES = {"low": BandType.LOWPASS, "lowpass": BandType.LOWPASS,
+                "high": BandType.HIGHPASS, "highpass": BandType.HIGHPASS,
+                "band": BandType.BANDPASS, "bandpass": BandType.BANDPASS,
+                "bandstop": BandType.BANDSTOP, "stop": BandType.BANDSTOP}
+
+
+def _cplx_pairs(v) -> np.ndarray:
+    v = np.asarray(v, np.complex128).ravel()
+    return np.ascontiguousarray(np.stack([v.real, v.imag], axis=1).ravel())
+
+
+def iirfilter(order: int, wn, btype="low", family: FilterFamily = FilterFamily.BUTTER,
+              rp: float = 0.0, fs: Optional[float] = None, output: str = "sos"):
+    """Digital IIR design (iirfilter, crates/scir-iir-filters/src/filter_design.rs:216-314).
+
+    ``wn`` is one edge or two increasing edges in the units of ``fs`` (normalised
+    to Nyquist = 1 when ``fs`` is None).  ``output`` is ``"sos"`` ([nsec, 6]) or
+    ``"zpk"`` (zeros, poles, gain).
+    """
+    bt = _BTYPE_NAMES[btype] if isinstance(btype, str) else BandType(btype)
+    w = np.ascontiguousarray(np.atleast_1d(np.asarray(wn, np.float64)))
+    need = 2 if bt >= BandType.BANDPASS else 1
+    if w.size != need:
+        raise GpuError(ERR_INVALID_ARG, f"{bt.name.lower()} needs {need} edge(s), got {w.size}")
+    fsv = -1.0 if fs is None else float(fs)
+    lib = load()
+    if output == "sos":
+        nsec = ctypes.c_int(0)
+        _check(lib.scir_iirfilter_sos(int(order), int(family), int(bt), _ptr(w), float(rp), fsv,
+                                      None, 0, ctypes.byref(nsec)))
+        sos = np.empty((nsec.value, 6), np.float64)
+        _check(lib.scir_iirfilter_sos(int(order), int(family), int(bt), _ptr(w), float(rp), fsv,
+                                      _ptr(sos), nsec.value, ctypes.byref(nsec)))
+        return sos
+    if output != "zpk":
+        raise GpuError(ERR_INVALID_ARG, f"unknown output {output!r}")
+    nz, npl, k = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0.0)
+    _check(lib.scir_iirfilter_zpk(int(order), int(family), int(bt), _ptr(w), float(rp), fsv,
+                                  None, None, 0, ctypes.byref(nz), ctypes.byref(npl),
+                                  ctypes.byref(k)))
+    cap = max(nz.value, npl.value, 1)
+    zb = np.empty(2 * cap, np.float64)
+    pb = np.empty(2 * cap, np.float64)
+    _check(lib.scir_iirfilter_zpk(int(order), int(family), int(bt), _ptr(w), float(rp), fsv,
+                                  _ptr(zb), _ptr(pb), cap, ctypes.byref(nz), ctypes.byref(npl),
+                                  ctypes.byref(k)))
+    z = zb[0:2 * nz.value:2] + 1j * zb[1:2 * nz.value:2]
+    p = pb[0:2 * npl.value:2] + 1j * pb[1:2 * npl.value:2]
+    return z, p, k.value
+
+
+def butter(order: int, wn, btype="low", fs: Optional[float] = None, output: str = "sos"):
+    """butter (crates/scir-iir-filters/src/filter_design.rs:128)."""
+    return iirfilter(order, wn, btype, FilterFamily.BUTTER, 0.0, fs, output)
+
+
+def cheby1(order: int, rp: float, wn, btype="low", fs: Optional[float] = None,
+           output: str = "sos"):
+    """cheby1 (crates/scir-iir-filters/src/filter_design.rs:191)."""
+    return iirfilter(order, wn, btype, FilterFamily.CHEBY1, rp, fs, output)
+
+
+def bessel(order: int, wn, btype="low", fs: Optional[float] = None, norm: str = "phase",
+           output: str = "sos"):
+    """bessel / bessel_with_norm (crates/scir-iir-filters/src/filter_design.rs:154-175)."""
+    fam = {"phase": FilterFamily.BESSEL_PHASE, "delay": FilterFamily.BESSEL_DELAY,
+           "mag": FilterFamily.BESSEL_MAG}[norm]
+    return iirfilter(order, wn, btype, fam, 0.0, fs, output)
+
+
+def zpk2sos(z, p, k: float, pairing: SosPairing = SosPairing.NEAREST) -> np.ndarray:
+    """zpk2sos (crates/scir-iir-filters/src/sos.rs:154-357)."""
+    zb, pb = _cplx_pairs(z), _cplx_pairs(p)
+    nz, npl = zb.size // 2, pb.size // 2
+    nsec = ctypes.c_int(0)
+    lib = load()
+    _check(lib.scir_zpk2sos(_ptr(zb), nz, _ptr(pb), npl, float(k), int(pairing), None, 0,
+                            ctypes.byref(nsec)))
+    sos = np.empty((nsec.value, 6), np.float64)
+    _check(lib.scir_zpk2sos(_ptr(zb), nz, _ptr(pb), npl, float(k), int(pairing), _ptr(sos),
+                            nsec.value, ctypes.byref(nsec)))
+    return sos
 
 
 # --------------------------------------------------------------------------- device layer

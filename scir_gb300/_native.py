@@ -64,6 +64,11 @@ SIGNATURES = {
     "scir_lfilter_f64": (_int, [_vp, _i64, _i64, _i64, _vp, _int, _vp, _int, _vp, _vp, _vp, _i64,
                                 _vp]),
     "scir_lfilter_zi": (_int, [_vp, _int, _vp, _int, _vp]),
+    "scir_iirfilter_zpk": (_int, [_int, _int, _int, _vp, ctypes.c_double, ctypes.c_double, _vp, _vp,
+                                  _int, _vp, _vp, _vp]),
+    "scir_zpk2sos": (_int, [_vp, _int, _vp, _int, ctypes.c_double, _int, _vp, _int, _vp]),
+    "scir_iirfilter_sos": (_int, [_int, _int, _int, _vp, ctypes.c_double, ctypes.c_double, _vp, _int,
+                                  _vp]),
     "scir_sosfiltfilt_default_padlen": (_i64, [_vp, _int]),
     "scir_sosfiltfilt_f32": (_int, [_vp, _i64, _i64, _i64, _vp, _int, _int, _i64, _int, _vp, _i64,
                                     _vp]),
