@@ -799,19 +799,22 @@ def run_ours(args):
     e2e = {"value": e2e_value, "unit": W.unit, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h} if (h2d or d2h) else None
 
-    # roofline of the dominant kernel (one launch per step)
-    kern_ms = statistics.mean(per_step) / getattr(W, "roofline_launches", W.launches_per_step)
+    # roofline of the dominant kernel: algorithmic work of one launch over the
+    # mean launch duration (a step of rl launches of the same kernel does rl
+    # launches' worth of the step's algorithmic bytes / flops)
+    rl = getattr(W, "roofline_launches", W.launches_per_step)
+    kern_ms = statistics.mean(per_step) / rl
     if W.bound == "hbm":
-        achieved = W.alg_bytes() / (kern_ms / 1e3) / 1e9
+        achieved = W.alg_bytes() / rl / (kern_ms / 1e3) / 1e9
         peak, unit = peaks["hbm_gbs"], "GB/s"
     elif W.bound == "fp64":
-        achieved = W.alg_flops() / (kern_ms / 1e3) / 1e12
+        achieved = W.alg_flops() / rl / (kern_ms / 1e3) / 1e12
         peak, unit = FP64_PEAK_TFLOPS, "TFLOP/s"
     elif W.bound == "tensor" and W.products() > 1:
-        achieved = W.alg_flops() / (kern_ms / 1e3) / 1e12
+        achieved = W.alg_flops() / rl / (kern_ms / 1e3) / 1e12
         peak, unit = peaks["bf16_tflops"], "TFLOP/s"
     else:
-        achieved = W.alg_flops() / (kern_ms / 1e3) / 1e12
+        achieved = W.alg_flops() / rl / (kern_ms / 1e3) / 1e12
         peak, unit = FP32_PEAK_TFLOPS, "TFLOP/s"
     traffic = profile_traffic(W.name)
     per_signal = None

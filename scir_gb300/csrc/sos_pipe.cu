@@ -70,43 +70,80 @@ __device__ __forceinline__ void cp_async_wait() {
 
 enum StreamKind { kSos = 0, kFwd = 1, kBwd = 2 };
 
-// One section's coefficients in registers (a warp's sections are fixed for
-// the launch): FP32 DF2T b0 b1 b2 a1 a2, and for coupled sections
-// sigma-1, omega, C1, C2, b0.
-struct RegSec {
-    float c[5];
-    float k[5];
-    bool coupled;
+// The coefficients of a warp's sections (fixed for the launch) live in
+// registers as the halves of packed pairs: section 2i in .x, 2i+1 in .y.
+// A coupled half holds sigma-1, omega, -omega, C1, C2, b0; a DF2T half
+// holds b0, b1, b2, -a1, -a2.  The negated values are exact.
+struct PairSec {
+    float2 f[6];
 };
 
-__device__ __forceinline__ RegSec reg_sec(const SosCoef& sc, int s) {
-    RegSec r;
-#pragma unroll
-    for (int j = 0; j < 5; ++j) {
-        r.c[j] = sc.cf[s][j];
-        r.k[j] = sc.cp[s][j];
+__device__ __forceinline__ void put_sec(PairSec& p, int half, const SosCoef& sc, int s,
+                                        bool coupled) {
+    float v[6];
+    if (coupled) {
+        v[0] = sc.cp[s][0];
+        v[1] = sc.cp[s][1];
+        v[2] = -sc.cp[s][1];
+        v[3] = sc.cp[s][2];
+        v[4] = sc.cp[s][3];
+        v[5] = sc.cp[s][4];
+    } else {
+        v[0] = sc.cf[s][0];
+        v[1] = sc.cf[s][1];
+        v[2] = sc.cf[s][2];
+        v[3] = -sc.cf[s][3];
+        v[4] = -sc.cf[s][4];
+        v[5] = 0.0f;
     }
-    r.coupled = sc.coupled[s] != 0;
-    return r;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        if (half == 0) p.f[j].x = v[j];
+        else p.f[j].y = v[j];
+    }
 }
 
-// The arithmetic of sos_sec (PREC 2 / 3) on register coefficients.  FORM:
-// 0 = FP32 DF2T, 1 = coupled, 2 = chosen per section (a warp whose sections
-// mix real and complex poles).
-template <int FORM>
-__device__ __forceinline__ float sec_step(const RegSec& r, float& s1, float& s2, float prev) {
+// The arithmetic of sos_sec (PREC 2 / 3) for one section, on half H of its
+// pair.  FORM: 0 = FP32 DF2T, 1 = coupled, 2 = chosen per section (a warp
+// whose sections mix real and complex poles).
+template <int FORM, int H>
+__device__ __forceinline__ float sec_step(const PairSec& r, bool coupled, float& s1, float& s2,
+                                          float prev) {
+    auto c = [&](int j) { return H == 0 ? r.f[j].x : r.f[j].y; };
     float out;
-    if (FORM == 1 || (FORM == 2 && r.coupled)) {
+    if (FORM == 1 || (FORM == 2 && coupled)) {
         const float u = s1, v = s2;
-        out = fmaf(r.k[2], u, fmaf(r.k[3], v, r.k[4] * prev));
-        s1 = u + fmaf(r.k[0], u, fmaf(-r.k[1], v, prev));
-        s2 = v + fmaf(r.k[1], u, r.k[0] * v);
+        out = fmaf(c(3), u, fmaf(c(4), v, c(5) * prev));
+        s1 = u + fmaf(c(0), u, fmaf(c(2), v, prev));
+        s2 = v + fmaf(c(1), u, c(0) * v);
     } else {
-        out = fmaf(r.c[0], prev, s1);
-        s1 = fmaf(-r.c[3], out, fmaf(r.c[1], prev, s2));
-        s2 = fmaf(-r.c[4], out, r.c[2] * prev);
+        out = fmaf(c(0), prev, s1);
+        s1 = fmaf(c(3), out, fmaf(c(1), prev, s2));
+        s2 = fmaf(c(4), out, c(2) * prev);
     }
     return out;
+}
+
+// Two sections of a warp run one sample apart in one packed (f32x2) step:
+// the first section at sample p (x = input) and the second at sample p - 1
+// (x = the first section's previous output).  Each half performs exactly the
+// operations of sec_step in the same order (fma.rn / mul.rn / add.rn per
+// element), so the outputs are bit-identical to the scalar cascade with half
+// the instructions.  S1 / S2 hold (s1, s2) of the two sections; FORM 0 or 1.
+template <int FORM>
+__device__ __forceinline__ float2 pair_step(const PairSec& r, float2& S1, float2& S2, float2 X) {
+    float2 Y;
+    if (FORM == 1) {
+        const float2 U = S1, V = S2;
+        Y = __ffma2_rn(r.f[3], U, __ffma2_rn(r.f[4], V, __fmul2_rn(r.f[5], X)));
+        S1 = __fadd2_rn(U, __ffma2_rn(r.f[0], U, __ffma2_rn(r.f[2], V, X)));
+        S2 = __fadd2_rn(V, __ffma2_rn(r.f[1], U, __fmul2_rn(r.f[0], V)));
+    } else {
+        Y = __ffma2_rn(r.f[0], X, S1);
+        S1 = __ffma2_rn(r.f[3], Y, __ffma2_rn(r.f[1], X, S2));
+        S2 = __ffma2_rn(r.f[4], Y, __fmul2_rn(r.f[2], X));
+    }
+    return Y;
 }
 
 struct PipeArgs {
@@ -155,11 +192,16 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
     __syncthreads();
 
     float s1[SPW], s2[SPW];
-    RegSec rc[SPW];
+    constexpr int NP = (SPW + 1) / 2;  // coefficient pairs of this warp
+    PairSec pc[NP];
+    bool cpl[SPW];
 #pragma unroll
     for (int i = 0; i < SPW; ++i) {
         const int s = warp * SPW + i;
-        rc[i] = reg_sec(sc, s);
+        // the coupled form serves complex-pole sections in FP32_COUPLED only
+        cpl[i] = PREC == 3 && sc.coupled[s] != 0;
+        put_sec(pc[i / 2], i % 2, sc, s, cpl[i]);
+        if (i % 2 == 0 && i + 1 == SPW) put_sec(pc[i / 2], 1, sc, s, cpl[i]);  // unused .y half
         s1[i] = 0.0f;
         s2[i] = 0.0f;
         if (!FF && a.zi && live && s < sc.nsec)
@@ -177,26 +219,64 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
     if (PREC == 3) {
         int nc = 0;
 #pragma unroll
-        for (int i = 0; i < SPW; ++i) nc += rc[i].coupled ? 1 : 0;
+        for (int i = 0; i < SPW; ++i) nc += cpl[i] ? 1 : 0;
         form = nc == SPW ? 1 : nc == 0 ? 0 : 2;
     }
+    // section i of the warp on one sample (i is a constant after unrolling)
+    auto step_i = [&](auto formc, int i, float v) {
+        constexpr int FORM = decltype(formc)::value;
+        return (i & 1) ? sec_step<FORM, 1>(pc[i >> 1], cpl[i], s1[i], s2[i], v)
+                       : sec_step<FORM, 0>(pc[i >> 1], cpl[i], s1[i], s2[i], v);
+    };
     // Filters tn samples of this lane's channel in place through the warp's
     // sections (a full tile fully unrolled, so the shared loads run ahead).
+    // Full tiles of an all-coupled warp with 2-4 sections go through its
+    // section pairs, one pass over the tile per pair: sample 0 of the first
+    // section alone, then 31 packed steps, then sample 31 of the second
+    // section alone.  Measured on GB300 (16,384 x 131,072, 8 sections): the
+    // coupled cascade 9.65 -> 9.12 ms; the DF2T form, whose two-operation
+    // recurrence the lockstep lengthens, 6.17 -> 9.44 ms, so it stays scalar.
+    // More sections per warp would spill registers.
+    constexpr bool kPaired = SPW >= 2 && SPW <= 4;
     auto filter_tile = [&](auto formc, float(*t)[kLd], int tn) {
         constexpr int FORM = decltype(formc)::value;
-        if (tn == kTT) {
+        if (FORM == 1 && kPaired && tn == kTT) {
+#pragma unroll
+            for (int i = 0; i < SPW / 2; ++i) {
+                const int sa = 2 * i, sb = 2 * i + 1;
+                float2 S1 = make_float2(s1[sa], s1[sb]), S2 = make_float2(s2[sa], s2[sb]);
+                float ya = sec_step<FORM, 0>(pc[i], cpl[sa], S1.x, S2.x, t[lane][0]);
+#pragma unroll
+                for (int p = 1; p < kTT; ++p) {
+                    const float2 Y = pair_step<FORM>(pc[i], S1, S2, make_float2(t[lane][p], ya));
+                    t[lane][p - 1] = Y.y;
+                    ya = Y.x;
+                }
+                t[lane][kTT - 1] = sec_step<FORM, 1>(pc[i], cpl[sb], S1.y, S2.y, ya);
+                s1[sa] = S1.x;
+                s1[sb] = S1.y;
+                s2[sa] = S2.x;
+                s2[sb] = S2.y;
+            }
+            if (SPW % 2) {
+#pragma unroll
+                for (int p = 0; p < kTT; ++p)
+                    t[lane][p] = sec_step<FORM, 0>(pc[NP - 1], cpl[SPW - 1], s1[SPW - 1],
+                                                   s2[SPW - 1], t[lane][p]);
+            }
+        } else if (tn == kTT) {
 #pragma unroll
             for (int p = 0; p < kTT; ++p) {
                 float v = t[lane][p];
 #pragma unroll
-                for (int i = 0; i < SPW; ++i) v = sec_step<FORM>(rc[i], s1[i], s2[i], v);
+                for (int i = 0; i < SPW; ++i) v = step_i(formc, i, v);
                 t[lane][p] = v;
             }
         } else {
             for (int p = 0; p < tn; ++p) {
                 float v = t[lane][p];
 #pragma unroll
-                for (int i = 0; i < SPW; ++i) v = sec_step<FORM>(rc[i], s1[i], s2[i], v);
+                for (int i = 0; i < SPW; ++i) v = step_i(formc, i, v);
                 t[lane][p] = v;
             }
         }
