@@ -14,7 +14,9 @@
 // whole (persistent) launch: each output's phase taps, shifted to the
 // output's place inside the lane's input window and pre-shifted by the
 // window's fixed misalignment so the window is read with 16-byte shared
-// loads.  A work item is CT channels (1, 2 or 4, sharing every lane's tap
+// loads; the products run as packed f32x2 FMAs, each lane keeping the sums
+// over even and odd window positions in the two halves of a register pair.
+// A work item is CT channels (1, 2 or 4, sharing every lane's tap
 // matrix) x IP periods (32, or 16 with four channels); the items' channel
 // windows stream into a 4-stage shared-memory ring, one bulk copy per channel
 // row clamped to [0, n) with the zero fill written by the lanes (TMA tensor
@@ -154,7 +156,9 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
     // window start inside the stage for this thread's first period (iteration 0)
     const int L0 = (warp * g.ppw + pl) * g.down + rel0 + shift;
     const int a = L0 & 3;
-    float T[P][JWA];
+    // T2[p][j/2] = taps (j, j+1) of output p: register pairs for the packed
+    // FMAs below
+    float2 T2[P][JWA / 2];
 #pragma unroll
     for (int p = 0; p < P; ++p) {
         const int rho = gl * P + p;
@@ -165,7 +169,9 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
         for (int j = 0; j < JWA; ++j) {
             const int q = d + g.Q - 1 + a - j;
             const int64_t hj = (int64_t)ph + (int64_t)q * g.up;
-            T[p][j] = (active && rho < g.up && q >= 0 && q < g.Q && hj < kh) ? __ldg(h + hj) : 0.0f;
+            const float v = (active && rho < g.up && q >= 0 && q < g.Q && hj < kh) ? __ldg(h + hj) : 0.0f;
+            if (j & 1) T2[p][j / 2].y = v;
+            else T2[p][j / 2].x = v;
         }
     }
 
@@ -188,35 +194,40 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
         for (int it = warp; it < iters; it += kNW) {
             const int po = it * g.ppw + pl;  // period offset inside the item
             const int La = (po * g.down + rel0 + shift) & ~3;
-            float acc[CT][P];
+            // acc2 = (sum over even window positions, sum over odd ones): one
+            // packed FMA (f32x2) per tap pair halves the FMA instructions
+            float2 acc2[CT][P];
 #pragma unroll
             for (int r = 0; r < CT; ++r)
 #pragma unroll
-                for (int p = 0; p < P; ++p) acc[r][p] = 0.0f;
+                for (int p = 0; p < P; ++p) acc2[r][p] = make_float2(0.0f, 0.0f);
             if (active) {
 #pragma unroll
                 for (int j4 = 0; j4 < JWA / 4; ++j4) {
                     // the same tap matrix serves every channel of the item
-                    float w[CT][4];
+                    float2 w[CT][2];
 #pragma unroll
                     for (int r = 0; r < CT; ++r) {
                         const float4 v =
                             reinterpret_cast<const float4*>(win + r * g.win_floats + La)[j4];
-                        w[r][0] = v.x;
-                        w[r][1] = v.y;
-                        w[r][2] = v.z;
-                        w[r][3] = v.w;
+                        w[r][0] = make_float2(v.x, v.y);
+                        w[r][1] = make_float2(v.z, v.w);
                     }
                     // consecutive FMAs update different accumulators
 #pragma unroll
-                    for (int e = 0; e < 4; ++e)
+                    for (int e = 0; e < 2; ++e)
 #pragma unroll
                         for (int r = 0; r < CT; ++r)
 #pragma unroll
                             for (int p = 0; p < P; ++p)
-                                acc[r][p] = fmaf(T[p][4 * j4 + e], w[r][e], acc[r][p]);
+                                acc2[r][p] = __ffma2_rn(T2[p][2 * j4 + e], w[r][e], acc2[r][p]);
                 }
             }
+            float acc[CT][P];
+#pragma unroll
+            for (int r = 0; r < CT; ++r)
+#pragma unroll
+                for (int p = 0; p < P; ++p) acc[r][p] = acc2[r][p].x + acc2[r][p].y;
             float* yb = ybuf + (warp * 2 + ybsel) * (32 * P * CT);
             const int64_t m0 = (i0 + (int64_t)it * g.ppw) * g.up;
             if (g.bulk) {
