@@ -7,7 +7,8 @@
 //    GpuError; it never changes the output shape (b x n).  It creates a CUDA
 //    context and loads a module per call; this layer keeps per-device
 //    streams and staging buffers alive instead and pipelines row chunks
-//    (copy in / filter / copy out on three streams).
+//    (copy in / filter / copy out on their own streams ordered by events,
+//    four chunks in flight).
 //  - sosfilt / filtfilt (crates/scir-signal/src/lib.rs:260-291) take f64 and
 //    start from a zero state; their host entry points use the exact FP64
 //    kernels.
@@ -146,14 +147,23 @@ int fill_sos(const double* sos, int nsec, bool want_zi, SosCoef* c) {
 
 // ---------------------------------------------------------------- staging pool
 // Per-device streams and grow-only device buffers for the host-buffer layer.
+// One stream per copy direction and one kernel stream per buffer carry the
+// stages of a row chunk (copy in, filter, copy out), and events order them,
+// so the two copy directions and the kernels overlap across kBufs chunks in
+// flight: a chunk's upload waits only for the kernel that last read its
+// input buffer, its kernel for its upload and for the download that last
+// read its output buffer.  Chunks' kernels may run concurrently (a chunk of
+// few rows does not fill the GPU).
 struct Stager {
-    static constexpr int kStreams = 3;
+    static constexpr int kBufs = 4;              // chunks in flight
+    static constexpr int kStreams = 2 + kBufs;   // copy in, copy out, kernels
     std::mutex mu;
     bool ready = false;
     cudaStream_t st[kStreams] = {};
-    void* din[kStreams] = {};
-    void* dout[kStreams] = {};
-    size_t cap_in[kStreams] = {}, cap_out[kStreams] = {};
+    cudaEvent_t ev_in[kBufs] = {}, ev_k[kBufs] = {}, ev_out[kBufs] = {};
+    void* din[kBufs] = {};
+    void* dout[kBufs] = {};
+    size_t cap_in[kBufs] = {}, cap_out[kBufs] = {};
     void* dtaps = nullptr;
     size_t cap_taps = 0;
 };
@@ -187,46 +197,73 @@ int stager_init(Stager* s) {
     if (s->ready) return SCIR_OK;
     for (int i = 0; i < Stager::kStreams; ++i)
         SCIR_CUDA_TRY(cudaStreamCreateWithFlags(&s->st[i], cudaStreamNonBlocking));
+    for (int i = 0; i < Stager::kBufs; ++i) {
+        SCIR_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_in[i], cudaEventDisableTiming));
+        SCIR_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_k[i], cudaEventDisableTiming));
+        SCIR_CUDA_TRY(cudaEventCreateWithFlags(&s->ev_out[i], cudaEventDisableTiming));
+    }
     s->ready = true;
     return SCIR_OK;
 }
 
 // Runs `body(chunk_rows, in_dev, out_dev, stream)` over row chunks with the
 // copies around it: rows [r, r+cr) of `hin` (row bytes in_row) go to in_dev,
-// out_dev (row bytes out_row) comes back into `hout`.
+// out_dev (row bytes out_row) comes back into `hout`.  Chunks hold ~64 MB;
+// `quantum` rounds the rows of a chunk up to a multiple that fills the
+// body's kernels (the tensor-core FIR tiles 128 channels) while a chunk
+// stays within 512 MB.
 template <typename Body>
 int pipeline_rows(Stager* s, const void* hin, size_t in_row, void* hout, size_t out_row,
-                  int64_t rows, Body body) {
-    const size_t target = 64ull << 20;
-    int64_t cr = (int64_t)(target / (in_row + out_row + 1));
+                  int64_t rows, Body body, int64_t quantum = 1) {
+    const size_t target = 64ull << 20, cap = 512ull << 20;
+    const size_t row_bytes = in_row + out_row + 1;
+    int64_t cr = (int64_t)(target / row_bytes);
     if (cr < 1) cr = 1;
+    if (quantum > 1) {
+        const int64_t cq = (cr + quantum - 1) / quantum * quantum;
+        if ((size_t)cq * row_bytes <= cap) cr = cq;
+    }
     if (cr > rows) cr = rows;
     const int64_t nchunks = ceil_div(rows, cr);
-    const int used = (int)(nchunks < Stager::kStreams ? nchunks : Stager::kStreams);
+    const int used = (int)(nchunks < Stager::kBufs ? nchunks : Stager::kBufs);
     for (int i = 0; i < used; ++i) {
         int rc = ensure(&s->din[i], &s->cap_in[i], (size_t)cr * in_row);
         if (rc) return rc;
         rc = ensure(&s->dout[i], &s->cap_out[i], (size_t)cr * out_row);
         if (rc) return rc;
     }
+    cudaStream_t s_in = s->st[0], s_out = s->st[1];
+    auto drain = [&]() {
+        for (int j = 0; j < Stager::kStreams; ++j) cudaStreamSynchronize(s->st[j]);
+    };
     for (int64_t c = 0; c < nchunks; ++c) {
-        const int i = (int)(c % Stager::kStreams);
+        const int i = (int)(c % Stager::kBufs);
+        const bool reuse = c >= Stager::kBufs;
+        cudaStream_t s_k = s->st[2 + i];
         const int64_t r0 = c * cr;
         const int64_t nr = (r0 + cr <= rows) ? cr : rows - r0;
-        cudaStream_t st = s->st[i];
+        // input buffer i: last read by the kernel of chunk c - kBufs
+        if (reuse) SCIR_CUDA_TRY(cudaStreamWaitEvent(s_in, s->ev_k[i], 0));
         if (in_row)
             SCIR_CUDA_TRY(cudaMemcpyAsync(s->din[i], (const char*)hin + (size_t)r0 * in_row,
-                                          (size_t)nr * in_row, cudaMemcpyHostToDevice, st));
-        int rc = body(nr, s->din[i], s->dout[i], st);
+                                          (size_t)nr * in_row, cudaMemcpyHostToDevice, s_in));
+        SCIR_CUDA_TRY(cudaEventRecord(s->ev_in[i], s_in));
+        SCIR_CUDA_TRY(cudaStreamWaitEvent(s_k, s->ev_in[i], 0));
+        // output buffer i: last read by the download of chunk c - kBufs
+        if (reuse) SCIR_CUDA_TRY(cudaStreamWaitEvent(s_k, s->ev_out[i], 0));
+        int rc = body(nr, s->din[i], s->dout[i], s_k);
         if (rc) {
-            for (int j = 0; j < Stager::kStreams; ++j) cudaStreamSynchronize(s->st[j]);
+            drain();
             return rc;
         }
+        SCIR_CUDA_TRY(cudaEventRecord(s->ev_k[i], s_k));
+        SCIR_CUDA_TRY(cudaStreamWaitEvent(s_out, s->ev_k[i], 0));
         if (out_row)
             SCIR_CUDA_TRY(cudaMemcpyAsync((char*)hout + (size_t)r0 * out_row, s->dout[i],
-                                          (size_t)nr * out_row, cudaMemcpyDeviceToHost, st));
+                                          (size_t)nr * out_row, cudaMemcpyDeviceToHost, s_out));
+        SCIR_CUDA_TRY(cudaEventRecord(s->ev_out[i], s_out));
     }
-    for (int j = 0; j < used; ++j) SCIR_CUDA_TRY(cudaStreamSynchronize(s->st[j]));
+    for (int j = 0; j < Stager::kStreams; ++j) SCIR_CUDA_TRY(cudaStreamSynchronize(s->st[j]));
     SCIR_CUDA_TRY(cudaGetLastError());
     return SCIR_OK;
 }
@@ -564,7 +601,8 @@ SCIR_API int scir_fir_batched_f32_host(const float* x, int64_t batch, int64_t n,
                              return scir_fir_batched_f32((const float*)din, n, nr, n,
                                                          (const float*)dt, k, mode, precision,
                                                          (float*)dout, n_out, st);
-                         });
+                         },
+                         128);
 }
 
 SCIR_API int scir_fir1d_batched_f32_cuda(const float* x, size_t b, size_t n, const float* taps,
