@@ -2,9 +2,14 @@
 three normalisations) and zpk2sos with the three pairings.
 
 Known answers are the reference's own tests (crates/scir-iir-filters/src/
-sos.rs:467-775, which hold Octave / MATLAB / SciPy values); the sweeps compare
-with scipy.signal, whose iirfilter / zpk2sos the reference follows.  No GPU.
+sos.rs:467-775, which hold Octave / MATLAB / SciPy values; filter_design.rs
+butter_internal tests, extracted into tests/golden/design_zpk.json) and the
+SOS designs in the reference's fixture file; the sweeps compare with
+scipy.signal, whose iirfilter / zpk2sos the reference follows.  No GPU.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -213,3 +218,55 @@ def test_sos_capacity_reported():
     assert lib.scir_iirfilter_sos(6, 0, 2, sg._ptr(wn), 0.0, -1.0, sg._ptr(buf), 5,
                                   ctypes.byref(nsec)) == sg.ERR_SHAPE
     assert not buf.any()
+
+
+# ------------------------------------------------ pinned by the reference's design tests
+_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+_DESIGN = json.load(open(os.path.join(_GOLDEN, "design_zpk.json")))
+_BT = {"LowPass": "low", "HighPass": "high", "BandPass": "bandpass", "BandStop": "bandstop"}
+
+
+def _sorted_c(v):
+    v = np.asarray(v, complex)
+    return v[np.lexsort((np.round(v.real, 9), np.round(v.imag, 9)))]
+
+
+@pytest.mark.parametrize("case", _DESIGN, ids=[c["name"] for c in _DESIGN])
+def test_butter_zpk_reference_known_answers(case):
+    """crates/scir-iir-filters/src/filter_design.rs butter_internal(N, ..., None) tests."""
+    z, p, k = sg.butter(case["order"], case["wn"], _BT[case["btype"]], output="zpk")
+    ze = np.array([complex(a, b) for a, b in case["z"]])
+    pe = np.array([complex(a, b) for a, b in case["p"]])
+    assert z.size == ze.size and p.size == pe.size
+    tol = case["tol"]
+    np.testing.assert_allclose(_sorted_c(z), _sorted_c(ze), atol=tol, rtol=0)
+    np.testing.assert_allclose(_sorted_c(p), _sorted_c(pe), atol=tol, rtol=0)
+    assert abs(k - case["k"]) <= tol * max(1.0, abs(case["k"]))
+
+
+@pytest.mark.parametrize("order", range(25))
+def test_butter_highpass_zeros_at_dc(order):
+    """filter_design.rs test_butter__basic_digital_z_plane: HighPass(0.01), N < 25."""
+    z, p, _ = sg.butter(order, 0.01, "high", output="zpk")
+    assert z.size == order and np.all(z == 1.0)
+    assert np.all(np.abs(p) <= 1.0)
+
+
+_FIXTURE_DESIGNS = {
+    # tests/golden/signal_fixtures.npz keys -> the design the reference's
+    # scripts/gen_signal_fixtures.py made them with (Wn normalised, no fs)
+    "butter_sos": lambda: sg.butter(4, 0.2),
+    "cheby_sos": lambda: sg.cheby1(4, 1.0, 0.2),
+    "bessel_sos": lambda: sg.bessel(4, 0.2),
+    "bessel_lp_delay_sos": lambda: sg.bessel(4, 0.2, norm="delay"),
+    "bessel_lp_mag_sos": lambda: sg.bessel(4, 0.2, norm="mag"),
+    "butter_hp_sos": lambda: sg.butter(4, 0.3, "high"),
+    "cheby_hp_sos": lambda: sg.cheby1(4, 1.0, 0.3, "high"),
+    "bessel_hp_sos": lambda: sg.bessel(4, 0.3, "high", norm="phase"),
+}
+
+
+@pytest.mark.parametrize("key", sorted(_FIXTURE_DESIGNS))
+def test_design_matches_reference_fixtures(key):
+    fx = np.load(os.path.join(_GOLDEN, "signal_fixtures.npz"))
+    np.testing.assert_allclose(_FIXTURE_DESIGNS[key](), fx[key], rtol=1e-11, atol=1e-14)
