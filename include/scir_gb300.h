@@ -365,6 +365,23 @@ SCIR_API int scir_iirfilter_sos(int order, int family, int btype,
                                 const double* wn, double rp, double fs,
                                 double* sos, int cap, int* nsec);
 
+/* FIR design (host, FP64): scipy.signal.firwin(numtaps, cutoff, window,
+ * pass_zero, scale, fs) for 1..64 increasing band edges (in the units of fs;
+ * fs <= 0: normalised to Nyquist = 1).  The reference bakes its one design
+ * as a table (crates/scir-signal/src/lib.rs:315-347); this gives the Rust/C
+ * callers the taps of every configuration without SciPy.  beta is read for
+ * SCIR_WIN_KAISER only.  A pass band at Nyquist needs odd numtaps. */
+enum scir_window {
+    SCIR_WIN_HAMMING = 0,
+    SCIR_WIN_KAISER = 1,
+    SCIR_WIN_HANN = 2,
+    SCIR_WIN_BLACKMAN = 3,
+    SCIR_WIN_BOXCAR = 4
+};
+SCIR_API int scir_firwin(int64_t numtaps, const double* cutoff, int ncut,
+                         int window, double beta, int pass_zero, int scale,
+                         double fs, double* h);
+
 /* ----------------------------------------------------------------------- */
 /* Second-order sections (device pointers, stream-ordered)                 */
 /* Replaces scir_signal::sosfilt / filtfilt (crates/scir-signal/src/lib.rs:*/

@@ -30,7 +30,7 @@ __all__ = [
     "upfirdn_out_len", "resample_poly_f32", "resample_poly_out_len", "resample_poly_default_taps",
     "sosfilt_f32", "sosfilt_f64", "sosfiltfilt_f32", "sosfiltfilt_f64", "sosfilt_zi",
     "sosfiltfilt_default_padlen", "RaggedPlan", "load", "device_errors", "FilterFamily", "BandType",
-    "SosPairing", "iirfilter", "butter", "cheby1", "bessel", "zpk2sos",
+    "SosPairing", "iirfilter", "butter", "cheby1", "bessel", "zpk2sos", "firwin",
 ]
 
 OK, ERR_INVALID_ARG, ERR_SHAPE, ERR_ALIGN, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED, \
@@ -465,6 +465,31 @@ def bessel(order: int, wn, btype="low", fs: Optional[float] = None, norm: str = 
     fam = {"phase": FilterFamily.BESSEL_PHASE, "delay": FilterFamily.BESSEL_DELAY,
            "mag": FilterFamily.BESSEL_MAG}[norm]
     return iirfilter(order, wn, btype, fam, 0.0, fs, output)
+
+
+_WINDOWS = {"hamming": 0, "kaiser": 1, "hann": 2, "hanning": 2, "blackman": 3, "boxcar": 4,
+            "rectangular": 4}
+
+
+def firwin(numtaps: int, cutoff, window="hamming", pass_zero=True, scale: bool = True,
+           fs: Optional[float] = None) -> np.ndarray:
+    """scipy.signal.firwin: window is a name or ("kaiser", beta); pass_zero is a
+    bool or "lowpass" / "highpass" / "bandpass" / "bandstop"."""
+    c = np.ascontiguousarray(np.atleast_1d(np.asarray(cutoff, np.float64)))
+    beta = 0.0
+    if isinstance(window, tuple):
+        name, beta = window[0], float(window[1])
+    else:
+        name = window
+    if name not in _WINDOWS:
+        raise GpuError(ERR_INVALID_ARG, f"unsupported window {window!r}")
+    if isinstance(pass_zero, str):
+        pass_zero = pass_zero in ("lowpass", "bandstop")
+    h = np.empty(int(numtaps), np.float64)
+    _check(load().scir_firwin(int(numtaps), _ptr(c), c.size, _WINDOWS[name], beta,
+                              1 if pass_zero else 0, 1 if scale else 0,
+                              -1.0 if fs is None else float(fs), _ptr(h)))
+    return h
 
 
 def zpk2sos(z, p, k: float, pairing: SosPairing = SosPairing.NEAREST) -> np.ndarray:

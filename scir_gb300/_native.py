@@ -69,6 +69,8 @@ SIGNATURES = {
     "scir_zpk2sos": (_int, [_vp, _int, _vp, _int, ctypes.c_double, _int, _vp, _int, _vp]),
     "scir_iirfilter_sos": (_int, [_int, _int, _int, _vp, ctypes.c_double, ctypes.c_double, _vp, _int,
                                   _vp]),
+    "scir_firwin": (_int, [_i64, _vp, _int, _int, ctypes.c_double, _int, _int, ctypes.c_double,
+                           _vp]),
     "scir_sosfiltfilt_default_padlen": (_i64, [_vp, _int]),
     "scir_sosfiltfilt_f32": (_int, [_vp, _i64, _i64, _i64, _vp, _int, _int, _i64, _int, _vp, _i64,
                                     _vp]),

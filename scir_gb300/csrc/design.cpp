@@ -176,3 +176,83 @@ int build_sos_coef(const double* sos, int nsec, bool want_zi, SosCoef* c) {
 }
 
 }  // namespace scir
+
+// ------------------------------------------------------------------ firwin
+// scipy.signal.firwin(numtaps, cutoff, window, pass_zero, scale, fs): the
+// published windowed-sinc construction for any set of band edges.  Edges are
+// normalised to Nyquist = 1; the pass bands are the intervals between
+// consecutive entries of [0 if pass_zero] + cutoff + [1 if the last band
+// reaches Nyquist]; h[i] = sum over bands of r sinc(r m) - l sinc(l m),
+// m = i - (numtaps - 1)/2, times a symmetric window; with `scale` the
+// response is set to 1 at the centre of the first pass band (0 if it starts
+// at DC, Nyquist if it ends there).
+namespace scir {
+namespace {
+
+double fir_window(int window, double beta, int64_t i, int64_t M) {
+    if (M == 1) return 1.0;
+    const double fac = -M_PI + (double)i * (2.0 * M_PI / (double)(M - 1));  // linspace(-pi, pi, M)
+    switch (window) {
+    case SCIR_WIN_HAMMING: return 0.54 + 0.46 * std::cos(fac);
+    case SCIR_WIN_HANN: return 0.5 + 0.5 * std::cos(fac);
+    case SCIR_WIN_BLACKMAN: return 0.42 + 0.5 * std::cos(fac) + 0.08 * std::cos(2.0 * fac);
+    case SCIR_WIN_BOXCAR: return 1.0;
+    default: {  // Kaiser: I0(beta sqrt(1 - (2i/(M-1) - 1)^2)) / I0(beta)
+        const double r = 2.0 * (double)i / (double)(M - 1) - 1.0;
+        const double arg = 1.0 - r * r;
+        return bessel_i0(beta * std::sqrt(arg > 0.0 ? arg : 0.0)) / bessel_i0(beta);
+    }
+    }
+}
+
+}  // namespace
+
+}  // namespace scir
+
+extern "C" SCIR_API int scir_firwin(int64_t numtaps, const double* cutoff, int ncut, int window,
+                                    double beta, int pass_zero, int scale, double fs,
+                                    double* h) {
+    using namespace scir;
+    clear_error();
+    SCIR_REQUIRE(numtaps >= 1, SCIR_ERR_INVALID_ARG, "numtaps must be >= 1");
+    SCIR_REQUIRE(cutoff && ncut >= 1 && ncut <= 64 && h, SCIR_ERR_INVALID_ARG,
+                 "need 1..64 cutoff frequencies and an output buffer");
+    SCIR_REQUIRE(window >= SCIR_WIN_HAMMING && window <= SCIR_WIN_BOXCAR, SCIR_ERR_INVALID_ARG,
+                 "unknown window %d", window);
+    const double nyq = fs > 0.0 ? 0.5 * fs : 1.0;
+    double edges[66];
+    int ne = 0;
+    if (pass_zero) edges[ne++] = 0.0;
+    for (int i = 0; i < ncut; ++i) {
+        const double c = cutoff[i] / nyq;
+        SCIR_REQUIRE(c > 0.0 && c < 1.0, SCIR_ERR_INVALID_ARG,
+                     "cutoff frequencies must be strictly between 0 and fs/2");
+        SCIR_REQUIRE(i == 0 || c > edges[ne - 1], SCIR_ERR_INVALID_ARG,
+                     "cutoff frequencies must increase");
+        edges[ne++] = c;
+    }
+    // the last band reaches Nyquist when the count of edges so far is odd
+    const bool pass_nyquist = (ne % 2) == 1;
+    SCIR_REQUIRE(!(pass_nyquist && numtaps % 2 == 0), SCIR_ERR_INVALID_ARG,
+                 "a filter with a pass band at Nyquist needs an odd number of taps");
+    if (pass_nyquist) edges[ne++] = 1.0;
+    const double alpha = 0.5 * (double)(numtaps - 1);
+    for (int64_t i = 0; i < numtaps; ++i) {
+        const double m = (double)i - alpha;
+        double v = 0.0;
+        for (int b = 0; b + 1 < ne; b += 2) {
+            const double l = edges[b], r = edges[b + 1];
+            v += r * sinc(r * m) - l * sinc(l * m);
+        }
+        h[i] = v * fir_window(window, beta, i, numtaps);
+    }
+    if (scale) {
+        const double l = edges[0], r = edges[1];
+        const double f = l == 0.0 ? 0.0 : r == 1.0 ? 1.0 : 0.5 * (l + r);
+        double s = 0.0;
+        for (int64_t i = 0; i < numtaps; ++i) s += h[i] * std::cos(M_PI * ((double)i - alpha) * f);
+        SCIR_REQUIRE(s != 0.0, SCIR_ERR_INVALID_ARG, "zero response at the scaling frequency");
+        for (int64_t i = 0; i < numtaps; ++i) h[i] /= s;
+    }
+    return SCIR_OK;
+}

@@ -270,3 +270,59 @@ _FIXTURE_DESIGNS = {
 def test_design_matches_reference_fixtures(key):
     fx = np.load(os.path.join(_GOLDEN, "signal_fixtures.npz"))
     np.testing.assert_allclose(_FIXTURE_DESIGNS[key](), fx[key], rtol=1e-11, atol=1e-14)
+
+
+# ------------------------------------------------------------------ firwin
+_FIRWIN_BANDS = [(0.2, True), ([0.1, 0.3], False), ([0.1, 0.3], True), (0.4, False),
+                 ([0.1, 0.2, 0.5, 0.7], True), ([0.1, 0.2, 0.5, 0.7], False)]
+_WINDOWS = ["hamming", ("kaiser", 8.6), ("kaiser", 5.0), "hann", "blackman", "boxcar"]
+
+
+@pytest.mark.parametrize("numtaps", [1, 2, 3, 31, 64, 101, 4095])
+@pytest.mark.parametrize("cutoff,pass_zero", _FIRWIN_BANDS)
+def test_firwin_matches_scipy(numtaps, cutoff, pass_zero):
+    import warnings
+    for window in _WINDOWS:
+        for scale in (True, False):
+            with warnings.catch_warnings():
+                warnings.simplefilter("ignore")
+                try:
+                    ref = ss.firwin(numtaps, cutoff, window=window, pass_zero=pass_zero, scale=scale)
+                except ValueError:
+                    ref = None
+            if ref is None or not np.isfinite(ref).all():
+                # SciPy refuses (a Nyquist band with even taps) or divides by
+                # a zero response; the library refuses both
+                with pytest.raises(sg.GpuError):
+                    sg.firwin(numtaps, cutoff, window=window, pass_zero=pass_zero, scale=scale)
+                continue
+            got = sg.firwin(numtaps, cutoff, window=window, pass_zero=pass_zero, scale=scale)
+            np.testing.assert_allclose(got, ref, rtol=0, atol=1e-13 * np.abs(ref).max(),
+                                       err_msg=f"{window} scale={scale}")
+
+
+def test_firwin_benchmark_designs():
+    # the designs of the short-tap, long-tap and resample configurations
+    np.testing.assert_allclose(sg.firwin(63, 0.2, window="hamming"),
+                               ss.firwin(63, 0.2, window="hamming"), rtol=0, atol=1e-16)
+    np.testing.assert_allclose(
+        sg.firwin(4095, [0.1, 0.3], window=("kaiser", 8.6), pass_zero=False),
+        ss.firwin(4095, [0.1, 0.3], window=("kaiser", 8.6), pass_zero=False), rtol=0, atol=1e-15)
+    np.testing.assert_allclose(sg.firwin(3201, 1.0 / 160, window=("kaiser", 5.0)) * 160,
+                               sg.resample_poly_default_taps(160, 147), rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(
+        sg.firwin(101, [100.0, 300.0], window="blackman", pass_zero="bandpass", fs=2000.0),
+        ss.firwin(101, [100.0, 300.0], window="blackman", pass_zero="bandpass", fs=2000.0),
+        rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("call", [
+    lambda: sg.firwin(0, 0.2),                         # no taps
+    lambda: sg.firwin(31, 1.0),                        # at Nyquist
+    lambda: sg.firwin(31, [0.3, 0.2], pass_zero=False),  # decreasing
+    lambda: sg.firwin(32, 0.2, pass_zero=False),       # high-pass with even taps
+    lambda: sg.firwin(31, 0.2, window="tukey"),        # window not offered
+])
+def test_firwin_errors(call):
+    with pytest.raises(sg.GpuError):
+        call()
