@@ -187,7 +187,12 @@ class Resample(Workload):
         self.n_out = S.resample_poly_out_len(self.N, self.UP, self.DOWN)
         self.y = torch.empty((self.B, self.n_out), device=dev)
         self.kh = S.resample_poly_default_taps(self.UP, self.DOWN).size
-        self.kernel = "poly_stream_kernel"
+        # BF16X3 runs the tensor-core polyphase (tap-operand build + the
+        # contraction: two launches per step)
+        tc = precision == S.Precision.BF16X3
+        self.kernel = "poly_tc_kernel" if tc else "poly_stream_kernel"
+        self.launches_per_step = 2 if tc else 1
+        self.roofline_launches = 1
 
     @classmethod
     def config(cls):

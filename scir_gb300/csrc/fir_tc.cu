@@ -455,9 +455,4 @@ int launch_fir_tc(const FirArgs& a, int terms, cudaStream_t st) {
     return launch_tc<3>(a, st);
 }
 
-bool poly_tc_supported(const PolyArgs&) { return false; }
-int launch_poly_tc(const PolyArgs&, int, cudaStream_t) {
-    return set_error(SCIR_ERR_UNSUPPORTED, "tensor-core polyphase not built");
-}
-
 }  // namespace scir

@@ -116,3 +116,79 @@ def test_resample_padded_output_rows(cuda, pad):
     ref = O.resample_poly_fast_f64(x.astype(np.float64), 160, 147, h)
     assert normwise_err(y.cpu().numpy(), ref) < TOL_FP32
     assert bool((big[:, n_out:] == 7.0).all())  # nothing written past the row end
+
+
+# ------------------------------------------------- tensor-core polyphase (BF16X3)
+# split-bf16 products (x1c1 + x1c2 + x2c1) with FP32 accumulation: each
+# operand keeps ~16 significant bits, so the stated bound of this form is
+# 2e-5 normwise (measured 7e-6 .. 1.0e-5 on ~21-tap phases)
+TOL_TC = 2e-5
+
+
+@pytest.mark.parametrize("up,down", [(160, 147), (3, 2), (5, 4)])
+@pytest.mark.parametrize("batch,n", [(3, 1000), (130, 20000), (256, 4100), (5, 4)])
+def test_resample_tc_vs_oracle(cuda, up, down, batch, n):
+    rng = np.random.default_rng(batch * 7 + n + up)
+    x = rng.standard_normal((batch, n)).astype(np.float32)
+    h32 = S.resample_poly_default_taps(up, down, design=0).astype(np.float32)
+    ref = O.resample_poly_fast_f64(x.astype(np.float64), up, down, h32.astype(np.float64))
+    y = S.resample_poly_f32(_dev(x, cuda), up, down, precision=S.Precision.BF16X3).cpu().numpy()
+    assert y.shape == ref.shape
+    err = normwise_err(y, ref)
+    print(f"tensor-core resample {up}/{down} {batch}x{n}: normwise error {err:.2e}")
+    assert err < TOL_TC
+
+
+def test_upfirdn_tc_short_filter(cuda):
+    rng = np.random.default_rng(5)
+    h = rng.standard_normal(64).astype(np.float32)
+    x = rng.standard_normal((129, 3000)).astype(np.float32)
+    ref = O.upfirdn_f64(h.astype(np.float64), x.astype(np.float64), 4, 1)
+    y = S.upfirdn(_dev(h, cuda), _dev(x, cuda), 4, 1, precision=S.Precision.BF16X3).cpu().numpy()
+    assert y.shape == ref.shape
+    assert normwise_err(y, ref) < TOL_TC
+
+
+def test_resample_tc_padded_rows(cuda):
+    import torch
+    rng = np.random.default_rng(9)
+    x = rng.standard_normal((140, 5000)).astype(np.float32)
+    xp = torch.zeros((140, 5004), device=cuda)
+    xp[:, :5000] = _dev(x, cuda)
+    n_out = S.resample_poly_out_len(5000, 160, 147)
+    ld = n_out + 12 + (-n_out) % 4  # a row pitch of whole 16-byte units
+    out = torch.full((140, ld), 7.0, device=cuda)
+    S.resample_poly_f32(xp[:, :5000], 160, 147, precision=S.Precision.BF16X3, out=out[:, :n_out])
+    h32 = S.resample_poly_default_taps(160, 147).astype(np.float32).astype(np.float64)
+    ref = O.resample_poly_fast_f64(x.astype(np.float64), 160, 147, h32)
+    got = out.cpu().numpy()
+    assert normwise_err(got[:, :n_out], ref) < TOL_TC
+    assert np.all(got[:, n_out:] == 7.0)  # the row padding is not written
+
+
+def test_resample_tc_refuses_unserved_shape(cuda):
+    # 2/3 with the default 61-tap design: a 32-output segment spans more than
+    # the 64-sample window, so the tensor-core path reports UNSUPPORTED rather
+    # than running anything else
+    x = np.zeros((4, 1000), np.float32)
+    with pytest.raises(S.GpuError):
+        S.resample_poly_f32(_dev(x, cuda), 2, 3, precision=S.Precision.BF16X3)
+    # input rows without a 16-byte pitch cannot be read by the tensor map
+    x = np.zeros((4, 1001), np.float32)
+    with pytest.raises(S.GpuError):
+        S.resample_poly_f32(_dev(x, cuda), 160, 147, precision=S.Precision.BF16X3)
+
+
+def test_resample_tc_cfg2_full_size(cuda):
+    import torch
+    g = torch.Generator(device=cuda).manual_seed(0)
+    x = torch.randn((256, 1048576), device=cuda, generator=g)
+    y = S.resample_poly_f32(x, 160, 147, precision=S.Precision.BF16X3)
+    assert y.shape == (256, 1141308)
+    rows = [0, 129, 255]
+    xs = x[rows].cpu().numpy().astype(np.float64)
+    h = S.resample_poly_default_taps(160, 147).astype(np.float32).astype(np.float64)
+    ref = O.resample_poly_fast_f64(xs, 160, 147, h)
+    err = normwise_err(y[rows].cpu().numpy(), ref)
+    print(f"tensor-core resample cfg2: normwise error {err:.2e}")
+    assert err < TOL_TC
