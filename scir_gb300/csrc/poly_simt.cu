@@ -28,7 +28,7 @@
 // lanes' 16-byte window reads over the shared-memory banks.  Each warp stages
 // its period's outputs in double-buffered shared memory and writes them back
 // with one bulk copy per channel row (per-lane stores when the output rows
-// are not 16-byte aligned).
+// are not 16-byte aligned), lane r issuing row r's copy.
 //
 // Generic kernel: one thread per output, taps and input through the
 // read-only cache (down > up, long phases, misaligned rows).
@@ -233,7 +233,7 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
             if (g.bulk) {
                 // the bulk copy issued from this buffer two iterations ago has
                 // finished reading it once at most one group is pending
-                if (lane == 0) bulk_wait_read1();
+                if (lane < CT) bulk_wait_read1();
                 __syncwarp();
             }
             if (active) {
@@ -247,18 +247,18 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
                 // staged outputs -> global by one bulk copy per channel row
                 fence_proxy_async_smem();
                 __syncwarp();
-                if (lane == 0) {
-                    // outputs [m0, m0 + valid) of each row; periods past the
-                    // row end (valid <= 0) write nothing
+                if (lane < CT) {
+                    // lane r copies row r (its own bulk group): outputs
+                    // [m0, m0 + valid); periods past the row end (valid <= 0)
+                    // write nothing
+                    const int r = lane;
                     const int64_t valid = min((int64_t)cnt, n_out - m0);
-                    if (valid > 0) {
+                    if (valid > 0 && r < rows) {
                         const int64_t v4 = valid & ~(int64_t)3;
-                        for (int r = 0; r < rows; ++r) {
-                            float* __restrict__ yr = y + (row0 + r) * ld_y;
-                            if (v4 > 0)
-                                bulk_store(yr + m0, yb + r * cnt, (uint32_t)(v4 * sizeof(float)));
-                            for (int64_t e = v4; e < valid; ++e) yr[m0 + e] = yb[r * cnt + e];
-                        }
+                        float* __restrict__ yr = y + (row0 + r) * ld_y;
+                        if (v4 > 0)
+                            bulk_store(yr + m0, yb + r * cnt, (uint32_t)(v4 * sizeof(float)));
+                        for (int64_t e = v4; e < valid; ++e) yr[m0 + e] = yb[r * cnt + e];
                     }
                     bulk_commit();
                 }
@@ -291,7 +291,7 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
             if (next < g.n_items) issue_warp(s, next);
         }
     }
-    if (g.bulk && lane == 0) bulk_wait_all();
+    if (g.bulk && lane < CT) bulk_wait_all();
 }
 
 __global__ void __launch_bounds__(256)
