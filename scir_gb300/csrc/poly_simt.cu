@@ -83,9 +83,10 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
 
     // Loads item `item` into stage s (called by a whole warp).  Row windows
     // that start 16-byte aligned come in as one bulk copy per row, clamped
-    // to [0, n); the lanes write the zeros outside the row and the last
-    // n % 4 samples first.  Otherwise lane 0 registers the bytes and the
-    // lanes issue the tensor boxes in parallel (zero fill by TMA).
+    // to [0, n), lane r copying row r; the lanes write the zeros outside
+    // the row and the last n % 4 samples first.  Otherwise lane 0 registers
+    // the bytes and the lanes issue the tensor boxes in parallel (zero fill
+    // by TMA).
     auto issue_warp = [&](int s, int64_t item) {
         const int64_t row0 = (item / g.items_per_row) * CT;
         const int64_t i0 = (item % g.items_per_row) * g.IP;
@@ -109,14 +110,13 @@ poly_stream_kernel(const __grid_constant__ CUtensorMap xmap, const float* __rest
             }
             __threadfence_block();
             __syncwarp();
-            if (lane == 0) {
-                const uint32_t bytes = (uint32_t)((hi4 - lo) * (int64_t)sizeof(float));
-                mbar_arrive_expect_tx(&full[s], bytes * (uint32_t)rows);
-                if (bytes > 0)
-                    for (int r = 0; r < rows; ++r)
-                        bulk_load(stages + s * g.stage_floats + r * g.win_floats + (lo - pos_a),
-                                  x + (row0 + r) * ld_x + lo, bytes, &full[s]);
-            }
+            const uint32_t bytes = (uint32_t)((hi4 - lo) * (int64_t)sizeof(float));
+            if (lane == 0) mbar_arrive_expect_tx(&full[s], bytes * (uint32_t)rows);
+            __syncwarp();
+            // lane r copies row r
+            if (bytes > 0 && lane < rows)
+                bulk_load(stages + s * g.stage_floats + lane * g.win_floats + (lo - pos_a),
+                          x + (row0 + lane) * ld_x + lo, bytes, &full[s]);
             return;
         }
         if (lane == 0)
