@@ -23,9 +23,8 @@
 // Measured on GB300 (256 x 1,048,576, 160/147): 0.767 ms, slower than the
 // FP32 streaming kernel (0.707 ms then, 0.595 ms now), so it runs only when
 // BF16X3 is asked for.  The tiles starve on their inputs: each reads 128 rows
-// x 256 bytes,
-// the 2.2x overlap of neighbouring windows is only partly caught by L2, and
-// three 40 KB stages per SM keep too few bytes in flight (a variant with
+// x 256 bytes, the 2.2x overlap of neighbouring windows is only partly caught
+// by L2, and three 40 KB stages per SM keep too few bytes in flight (a variant with
 // four stages and per-thread output stores measured 1.55 ms: tensor pipe
 // 3.6 % busy, long-scoreboard stalls 13 per instruction, DRAM 21 %).
 //
