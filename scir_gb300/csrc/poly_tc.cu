@@ -183,6 +183,7 @@ poly_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
     if (warp == 0) {
         // ---------------------------------------------------------- producer
         if (lane == 0) {
+            int64_t issued = 0;
             for (int64_t k = 0;; ++k) {
                 const int64_t item = blockIdx.x + k * gridDim.x;
                 if (item >= g.n_items) break;
@@ -200,12 +201,18 @@ poly_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
                 tma_load_2d(xs + s * kXBytes + kXHalf, &xmap, &full[s], (int32_t)(lo + 32),
                             (int32_t)row0);
                 bulk_load(bs + s * kBBytes, table + (size_t)v * (kBBytes / 2), kBBytes, &full[s]);
+                ++issued;
             }
+            // copies still in flight (only after a timeout) land before the
+            // CTA leaves: the last use of each stage completes its phase
+            for (int64_t k = issued > kStages ? issued - kStages : 0; k < issued; ++k)
+                mbar_wait(&full[k % kStages], (uint32_t)((k / kStages) & 1));
         }
     } else if (warp == 1) {
         // ---------------------------------------------------------- MMA issuer
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16_f32(kM, kN);
+            int64_t issued = 0;
             for (int64_t k = 0;; ++k) {
                 const int64_t item = blockIdx.x + k * gridDim.x;
                 if (item >= g.n_items) break;
@@ -234,7 +241,12 @@ poly_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__
                 tc_commit(&empty[s]);    // window stage and tap variant free
                 tc_commit(&a_empty[b]);  // operand buffer free
                 tc_commit(&d_full[b]);   // accumulator ready
+                ++issued;
             }
+            // the last tile's MMAs finish before TMEM is released (they have
+            // already, unless a wait timed out)
+            if (issued > 0)
+                mbar_wait(&d_full[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1));
         }
     } else if (warp < 6) {
         // ---------------------------------------------------------- converters
