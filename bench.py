@@ -851,8 +851,7 @@ def run_ours(args):
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded torch.randn on the device)",
-        "config": dict(W.config(), channels=getattr(W, "B", None), precision=prec.name,
-                       parallelism=f"replicas x{world}"),
+        "config": run_config(W, prec, world),
         "roofline": {"bound": W.bound, "achieved": achieved, "peak": peak, "unit": unit,
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": W.kernel, "kernel_ms": kern_ms,
@@ -868,6 +867,17 @@ def run_ours(args):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def run_config(W, prec, world):
+    """The workload's configuration as run: the class describes its default
+    size, and --channels overrides the channel count."""
+    cfg = dict(W.config(), channels=getattr(W, "B", None), precision=prec.name,
+               parallelism=f"replicas x{world}")
+    default = getattr(type(W), "B", None)
+    if cfg["channels"] is not None and default is not None and cfg["channels"] != default:
+        cfg["workload"] += f" (run with {cfg['channels']} channels instead of {default})"
+    return cfg
 
 
 def main():
