@@ -790,7 +790,8 @@ def run_ours(args):
 
     # end to end through the host-buffer C-ABI call
     h2d, d2h = W.host_setup()
-    W.host_step()
+    for _ in range(max(1, args.warmup)):  # staging buffers, pinned pages, tuning: untimed
+        W.host_step()
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
