@@ -218,9 +218,9 @@ SCIR_API int64_t scir_resample_poly_out_len(int64_t n, int up, int down);
 /* Default anti-aliasing design for resample_poly, computed on the host in
  * FP64 and already multiplied by the reduced `up`:
  *   design 0 (SciPy): firwin(2*10*max(up,down)+1, 1/max, ('kaiser', 5.0));
- *   design 1 (reference): the reference's baked 2/3 table, which is
- *   firwin(31, 1/3, 'hamming') * 2 (crates/scir-signal/src/lib.rs:315-347);
- *   only up/down = 2/3 (after reduction) is accepted.
+ *   design 1 (reference): the reference's baked 31-value 2/3 table, the
+ *   same doubles bit for bit (crates/scir-signal/src/lib.rs:315-347); only
+ *   up/down = 2/3 (after reduction) is accepted.
  * Writes at most `cap` taps to h (host) and the count to *kh. */
 SCIR_API int scir_resample_poly_default_taps(int up, int down, int design,
                                              double* h, int64_t cap,

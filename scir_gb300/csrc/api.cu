@@ -87,6 +87,25 @@ struct TapBuf {
 std::mutex g_tap_mutex;
 std::map<TapKey, TapBuf> g_taps;
 
+// The reference's baked resample_poly(2, 3) filter, gain 2 included
+// (crates/scir-signal/src/lib.rs:315-347).  The values are the reference's
+// decimal literals, which C and Rust both round to the nearest double, so
+// the taps -- and every output of the exact FP64 path -- are the reference's
+// bit for bit.  (A firwin(31, 1/3, 'hamming') * 2 design agrees only to
+// ~1e-16 and changes the last bit of most outputs.)
+constexpr double kRefResample23[31] = {
+    2.074505559623708e-18,  3.538600036880219e-3,   5.068355234374961e-3,
+    -4.352628574659906e-18, -1.161274884414711e-2,  -1.705404264360788e-2,
+    1.031683205857806e-17,  3.382730607794791e-2,   4.62174845519145e-2,
+    -1.768899299634197e-17, -8.47200828101812e-2,   -1.166001508003416e-1,
+    2.365319648026013e-17,  2.641261112200551e-1,   5.446004399706618e-1,
+    6.652174560128868e-1,   5.446004399706618e-1,   2.641261112200551e-1,
+    2.365319648026013e-17,  -1.166001508003416e-1,  -8.472008281018122e-2,
+    -1.768899299634197e-17, 4.621748455191452e-2,   3.382730607794793e-2,
+    1.031683205857806e-17,  -1.70540426436079e-2,   -1.161274884414712e-2,
+    -4.352628574659906e-18, 5.068355234374964e-3,   3.538600036880219e-3,
+    2.074505559623708e-18};
+
 int default_taps_host(int up, int down, int design, std::vector<double>& h) {
     const int64_t g = gcd64(up, down);
     up = (int)(up / g);
@@ -95,8 +114,8 @@ int default_taps_host(int up, int down, int design, std::vector<double>& h) {
         if (up != 2 || down != 3)
             return set_error(SCIR_ERR_UNSUPPORTED,
                              "the reference resample_poly design exists only for up=2, down=3");
-        h.resize(31);
-        firwin_lowpass(31, 1.0 / 3.0, 0, 0.0, h.data());
+        h.assign(kRefResample23, kRefResample23 + 31);
+        return SCIR_OK;  // the table already carries the gain
     } else if (design == 0) {
         const int mr = up > down ? up : down;
         const int64_t nt = 2 * 10 * (int64_t)mr + 1;

@@ -31,6 +31,15 @@ def golden_strain():
 
 
 @pytest.fixture(scope="session")
+def golden_resample23():
+    """The reference's baked resample_poly(2, 3) table as literal text and
+    IEEE-754 bits (tests/golden/make_resample_golden.py)."""
+    import json
+    with open(os.path.join(GOLDEN, "resample23_table.json")) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="session")
 def cuda():
     """The CUDA device; a GPU test fails (never skips) when it is missing."""
     import torch

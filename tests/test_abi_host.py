@@ -63,10 +63,15 @@ def test_resample_cfg_output_length():
     assert S.resample_poly_out_len(1048576, 160, 147) == 1141308
 
 
-def test_reference_design_is_hamming_31():
+def test_reference_design_is_the_reference_table(golden_resample23):
+    # crates/scir-signal/src/lib.rs:315-347: the same 31 doubles, bit for bit
     h = S.resample_poly_default_taps(2, 3, design=1)
-    np.testing.assert_allclose(h, ss.firwin(31, 1 / 3, window="hamming") * 2, atol=1e-16, rtol=1e-13)
     assert h.size == 31
+    assert [int(b) for b in h.view(np.uint64)] == golden_resample23["bits"]
+    assert np.array_equal(h, np.array([float(s) for s in golden_resample23["literals"]]))
+    # the table is a Hamming design; it agrees with SciPy's only to ~1e-16
+    np.testing.assert_allclose(h, ss.firwin(31, 1 / 3, window="hamming") * 2, atol=1e-15, rtol=0)
+    assert S.resample_poly_default_taps(4, 6, design=1).tobytes() == h.tobytes()
 
 
 @pytest.mark.parametrize("up,down", [(160, 147), (2, 3), (3, 2), (1, 5), (4, 6)])

@@ -96,9 +96,9 @@ def test_sosfilt_and_filtfilt_fixtures(golden_signal):
 
 
 # crates/scir-signal/src/lib.rs:655-668: the reference resample_poly(2,3)
-# (31-tap Hamming design) matches SciPy's 61-tap default only to 2e-2
-def test_resample_reference_fixture(golden_signal):
-    h = ss.firwin(31, 1.0 / 3.0, window="hamming") * 2
+# (its baked 31-value table) matches SciPy's 61-tap default only to 2e-2
+def test_resample_reference_fixture(golden_signal, golden_resample23):
+    h = np.array([float(s) for s in golden_resample23["literals"]])
     y = O.resample_poly_ref_f64(golden_signal["sosfilt_input"], 2, 3, h)[0]
     exp = golden_signal["resample_poly_output"]
     assert y.shape == exp.shape

@@ -74,10 +74,12 @@ def test_resample_explicit_taps_and_copy(cuda):
     assert np.array_equal(y, x)
 
 
-def test_reference_resample_poly_2_3_bit_identical(cuda, golden_signal):
-    # crates/scir-signal/src/lib.rs:313-362 with its own design, f64
+def test_reference_resample_poly_2_3_bit_identical(cuda, golden_signal, golden_resample23):
+    # crates/scir-signal/src/lib.rs:313-362 with its own 31-value table (the
+    # literals extracted from the reference source), f64, through the
+    # restated zero-stuff / full convolution / decimate loop
     x = golden_signal["sosfilt_input"]
-    h = S.resample_poly_default_taps(2, 3, design=1)
+    h = np.array([float(s) for s in golden_resample23["literals"]])
     ref = O.resample_poly_ref_f64(x, 2, 3, h)[0]
     y = S.resample_poly(x, 2, 3)
     assert np.array_equal(y, ref)
@@ -86,6 +88,10 @@ def test_reference_resample_poly_2_3_bit_identical(cuda, golden_signal):
     rng = np.random.default_rng(4)
     xb = rng.standard_normal((3, 5001))
     assert np.array_equal(S.resample_poly(xb, 2, 3), O.resample_poly_ref_f64(xb, 2, 3, h))
+    # ragged lengths around the decimation period, and a long row
+    for n in (1, 2, 3, 4, 5, 31, 32, 33, 100003):
+        xr = rng.standard_normal((2, n))
+        assert np.array_equal(S.resample_poly(xr, 2, 3), O.resample_poly_ref_f64(xr, 2, 3, h)), n
     with pytest.raises(S.GpuError):
         S.resample_poly(xb, 160, 147)
 
