@@ -141,12 +141,29 @@ SCIR_API int scir_device_count(int* count);
  * since the last call.  Synchronises with the device.  The reference has no
  * device-side failure reporting (its CUDA path cannot run at all). */
 SCIR_API int scir_device_errors(unsigned* code);
+/* Self-test of the bounded-wait failure path on the current device (no
+ * reference counterpart: the reference has no device-side failure
+ * reporting).  A two-warp pipeline copies n_chunks chunks of 1,024 floats
+ * from `in` (device, 16-byte aligned) through a 4-stage shared-memory ring
+ * with cp.async.bulk / mbarriers and writes each chunk's sum to out[chunk].
+ * The producer issues only the first issue_chunks (<= n_chunks) chunks; if
+ * that is fewer, the consumer's wait for the next chunk gives up after
+ * wait_limit_cycles SM cycles (1e3 .. 4e9) and the kernel records
+ * SCIR_ERR_TIMEOUT's device code (1) in the device error word, as every
+ * TMA pipeline of the library does, and returns with no copy in flight;
+ * scir_device_errors() then reports it.  Asynchronous on `stream`. */
+SCIR_API int scir_selftest_pipeline(const float* in, int64_t n_chunks, int64_t issue_chunks,
+                                    long long wait_limit_cycles, float* out, void* stream);
 /* Scratch memory (split operands of the tensor-core FIR, filtfilt edge
  * extensions) comes from a per-device stream-ordered pool that keeps freed
  * memory for the next call.  This synchronises the current device and
  * returns the pool's unused memory.  No reference counterpart (the reference
  * allocates and frees device buffers on every call). */
 SCIR_API int scir_release_scratch(void);
+/* Bytes the current device's scratch pool holds (reserved) and hands out
+ * (used) right now; both 0 before the first call that needed scratch.  Does
+ * not create the pool.  No reference counterpart. */
+SCIR_API int scir_scratch_usage(uint64_t* reserved, uint64_t* used);
 
 /* ----------------------------------------------------------------------- */
 /* Batched FIR (device pointers, stream-ordered)                           */
@@ -433,8 +450,10 @@ SCIR_API int scir_sosfiltfilt_f64(const double* x, int64_t ld_x, int64_t batch,
  * counterpart in the reference.  The edge-extension scratch comes from a
  * fixed file-scope device array of 4 Mi floats (16 MiB, held on every device
  * that loads the library until the process exits); batch * padlen above that
- * is rejected with SCIR_ERR_SHAPE.  The first call on a device looks the
- * array's address up, so make it before any stream capture.  All calls share
+ * is rejected with SCIR_ERR_SHAPE.  The first call on a device looks up the
+ * addresses of the array and of the library's device error word (also a
+ * file-scope device variable), so make it before any stream capture.  No
+ * precision or padtype allocates.  All calls share
  * the array: calls that overlap on the GPU race and must be serialised by the
  * caller.  Arguments and results are those of scir_sosfiltfilt_f32. */
 SCIR_API int scir_sosfiltfilt_f32_noalloc(const float* x, int64_t ld_x, int64_t batch,

@@ -325,6 +325,14 @@ def release_scratch() -> None:
     _check(load().scir_release_scratch())
 
 
+def scratch_usage() -> tuple:
+    """(reserved, used) bytes of the library's scratch pool on the current
+    device; (0, 0) before any call needed scratch."""
+    r, u = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    _check(load().scir_scratch_usage(ctypes.byref(r), ctypes.byref(u)))
+    return int(r.value), int(u.value)
+
+
 def fir_out_len(n: int, k: int, mode: FirMode) -> int:
     v = int(load().scir_fir_out_len(n, k, int(mode)))
     if v < 0:

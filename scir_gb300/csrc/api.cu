@@ -13,8 +13,8 @@
 //    start from a zero state; their host entry points use the exact FP64
 //    kernels.
 //  - resample_poly (crates/scir-signal/src/lib.rs:313-362) accepts only
-//    up=2/down=3 and uses firwin(31, 1/3, 'hamming')*2; its host entry point
-//    keeps that restriction and that design, computed in FP64 with the
+//    up=2/down=3 and uses a baked 31-value table; its host entry point keeps
+//    that restriction and those doubles, computed in FP64 with the
 //    reference's summation order.
 #include "common.cuh"
 #include "kernels.cuh"
@@ -544,27 +544,39 @@ SCIR_API int scir_sosfilt_f64(const double* x, int64_t ld_x, int64_t batch, int6
 
 }  // extern "C"
 
-template <typename T>
-static int sosfiltfilt_impl(const T* x, int64_t ld_x, int64_t batch, int64_t n, const double* sos,
-                            int nsec, int padtype, int64_t padlen, int precision, T* y,
-                            int64_t ld_y, void* stream) {
-    clear_error();
+// Argument checks shared by every sosfiltfilt entry point (the allocating
+// ones and scir_sosfiltfilt_f32_noalloc): the padtype, the sections (and
+// their sosfilt_zi when padding), the rows, the in-place rule and the edge
+// length; then the current device.  Fills *c and the edge length *edge.
+int scir::sosfiltfilt_check(const void* x, int64_t ld_x, int64_t batch, int64_t n,
+                            const double* sos, int nsec, int padtype, int64_t padlen,
+                            const void* y, int64_t ld_y, SosCoef* c, int64_t* edge) {
     SCIR_REQUIRE(padtype == SCIR_PAD_NONE || padtype == SCIR_PAD_ODD, SCIR_ERR_INVALID_ARG,
                  "unknown padtype %d", padtype);
-    SosCoef c;
-    int rc = fill_sos(sos, nsec, padtype == SCIR_PAD_ODD, &c);
+    int rc = fill_sos(sos, nsec, padtype == SCIR_PAD_ODD, c);
     if (rc) return rc;
     rc = check_rows(x, ld_x, batch, n, y, ld_y, n);
     if (rc) return rc;
     SCIR_REQUIRE(y == x ? ld_y == ld_x : true, SCIR_ERR_INVALID_ARG,
                  "in-place sosfiltfilt needs ld_y == ld_x");
-    int64_t edge = 0;
-    if (padtype == SCIR_PAD_ODD) edge = padlen < 0 ? sos_default_padlen(sos, nsec) : padlen;
-    SCIR_REQUIRE(batch == 0 || n > edge, SCIR_ERR_SHAPE,
+    *edge = 0;
+    if (padtype == SCIR_PAD_ODD) *edge = padlen < 0 ? sos_default_padlen(sos, nsec) : padlen;
+    SCIR_REQUIRE(*edge >= 0, SCIR_ERR_INVALID_ARG, "negative padlen");
+    SCIR_REQUIRE(batch == 0 || n > *edge, SCIR_ERR_SHAPE,
                  "the signal must be longer than padlen (n=%lld, padlen=%lld)", (long long)n,
-                 (long long)edge);
+                 (long long)*edge);
     const DeviceInfo* info = nullptr;
-    rc = current_device(&info);
+    return current_device(&info);
+}
+
+template <typename T>
+static int sosfiltfilt_impl(const T* x, int64_t ld_x, int64_t batch, int64_t n, const double* sos,
+                            int nsec, int padtype, int64_t padlen, int precision, T* y,
+                            int64_t ld_y, void* stream) {
+    clear_error();
+    SosCoef c;
+    int64_t edge = 0;
+    int rc = sosfiltfilt_check(x, ld_x, batch, n, sos, nsec, padtype, padlen, y, ld_y, &c, &edge);
     if (rc) return rc;
     if (batch == 0 || n == 0) return SCIR_OK;
     cudaStream_t st = as_stream(stream);

@@ -86,6 +86,12 @@ int launch_sosfiltfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const
                        int64_t edge, int use_zi, int precision, T* y, int64_t ld_y,
                        T* tail_scratch, cudaStream_t st);
 
+// Argument checks of the sosfiltfilt entry points (api.cu): fills *c and the
+// edge-extension length *edge, and initialises the current device.
+int sosfiltfilt_check(const void* x, int64_t ld_x, int64_t batch, int64_t n, const double* sos,
+                      int nsec, int padtype, int64_t padlen, const void* y, int64_t ld_y,
+                      SosCoef* c, int64_t* edge);
+
 // Host-side FP64 design helpers (design.cpp).
 int sos_zi_host(const double* sos, int nsec, double* zi);
 int64_t sos_default_padlen(const double* sos, int nsec);

@@ -20,14 +20,16 @@
 //  - the array lives in every device that loads the library until the process
 //    exits;
 //  - the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (once per device, with that device current); make
-//    that first call before any stream capture;
+//    cudaGetSymbolAddress (once per device, with that device current), and
+//    the address of the library's device error word, which is a file-scope
+//    device variable too; make that first call before any stream capture;
 //  - every call shares the one array: calls that overlap on the GPU (other
 //    streams, other host threads) race on it and must be serialised by the
 //    caller.  Nothing in it needs to start at zero: each call writes every
 //    scratch element it reads before reading it.
 #include "common.cuh"
 #include "kernels.cuh"
+#include "sm100.cuh"
 
 #include <mutex>
 
@@ -42,7 +44,11 @@ constexpr int kMaxDev = 64;
 std::mutex g_noalloc_mutex;
 float* g_noalloc_ptr[kMaxDev] = {};
 
-// Device address of the array on the current device (looked up once).
+// Device address of the array on the current device, looked up once per
+// device with that device current.  The same first call also looks up the
+// library's device error word (a file-scope device variable as well, which
+// the FP32 pipeline kernels report bounded-wait timeouts to), so after the
+// first call nothing on this path touches the CUDA runtime's symbol tables.
 int noalloc_scratch(float** out) {
     int dev = 0;
     SCIR_CUDA_TRY(cudaGetDevice(&dev));
@@ -56,6 +62,8 @@ int noalloc_scratch(float** out) {
             return set_error(SCIR_ERR_CUDA, "cudaGetSymbolAddress(noalloc scratch): %s",
                              cudaGetErrorString(e));
         }
+        if (!device_error_word())
+            return set_error(SCIR_ERR_CUDA, "device error word unavailable");
         g_noalloc_ptr[dev] = static_cast<float*>(p);
     }
     *out = g_noalloc_ptr[dev];
@@ -72,32 +80,14 @@ extern "C" SCIR_API int scir_sosfiltfilt_f32_noalloc(const float* x, int64_t ld_
                                                      int padtype, int64_t padlen, int precision,
                                                      float* y, int64_t ld_y, void* stream) {
     clear_error();
-    SCIR_REQUIRE(padtype == SCIR_PAD_NONE || padtype == SCIR_PAD_ODD, SCIR_ERR_INVALID_ARG,
-                 "unknown padtype %d", padtype);
-    SCIR_REQUIRE(sos != nullptr, SCIR_ERR_INVALID_ARG, "sos is NULL");
-    SCIR_REQUIRE(nsec >= 1 && nsec <= SCIR_SOS_MAX_SECTIONS, SCIR_ERR_INVALID_ARG,
-                 "nsec %d not in [1, %d]", nsec, SCIR_SOS_MAX_SECTIONS);
-    SCIR_REQUIRE(batch >= 0 && n >= 0, SCIR_ERR_INVALID_ARG, "negative batch or length");
-    SCIR_REQUIRE(ld_x >= n && ld_y >= n, SCIR_ERR_SHAPE, "row stride shorter than the row");
-    if (batch > 0 && n > 0) SCIR_REQUIRE(x && y, SCIR_ERR_INVALID_ARG, "NULL buffer");
-    SCIR_REQUIRE(y == x ? ld_y == ld_x : true, SCIR_ERR_INVALID_ARG,
-                 "in-place sosfiltfilt needs ld_y == ld_x");
+    SosCoef c;  // host memory only
     int64_t edge = 0;
-    if (padtype == SCIR_PAD_ODD) edge = padlen < 0 ? sos_default_padlen(sos, nsec) : padlen;
-    SCIR_REQUIRE(edge >= 0, SCIR_ERR_INVALID_ARG, "negative padlen");
-    SCIR_REQUIRE(batch == 0 || n > edge, SCIR_ERR_SHAPE,
-                 "the signal must be longer than padlen (n=%lld, padlen=%lld)", (long long)n,
-                 (long long)edge);
+    int rc = sosfiltfilt_check(x, ld_x, batch, n, sos, nsec, padtype, padlen, y, ld_y, &c, &edge);
+    if (rc) return rc;
     SCIR_REQUIRE(edge == 0 || batch <= (int64_t)(kNoallocScratchFloats / (size_t)edge),
                  SCIR_ERR_SHAPE,
                  "batch * padlen = %lld * %lld exceeds the fixed scratch of %zu floats",
                  (long long)batch, (long long)edge, kNoallocScratchFloats);
-    SosCoef c;  // host memory only
-    if (build_sos_coef(sos, nsec, padtype == SCIR_PAD_ODD, &c) != SCIR_OK)
-        return set_error(SCIR_ERR_INVALID_ARG, "sosfilt_zi: a section has a pole at z=1");
-    const DeviceInfo* info = nullptr;
-    int rc = current_device(&info);
-    if (rc) return rc;
     float* tail = nullptr;
     rc = noalloc_scratch(&tail);
     if (rc) return rc;

@@ -199,7 +199,12 @@ int make_tmap_3d(CUtensorMap* map, CUtensorMapDataType dtype, const void* base, 
     return tmap_encode(map, dtype, 3, base, dims, strides, box, swizzle);
 }
 
+// The error word is a file-scope device variable (zero when the module
+// loads), so no entry point ever allocates device memory for it.  Host code
+// cannot use the symbol itself as a device address: its address on each
+// device is looked up once, with that device current.
 namespace {
+__device__ unsigned g_device_err_word = 0u;
 std::mutex g_err_mutex;
 unsigned* g_err_word[kMaxDevices] = {};
 }  // namespace
@@ -212,14 +217,12 @@ unsigned* device_error_word() {
     }
     std::lock_guard<std::mutex> lk(g_err_mutex);
     if (!g_err_word[dev]) {
-        unsigned* p = nullptr;
-        if (cudaMalloc(&p, sizeof(unsigned)) != cudaSuccess) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_device_err_word) != cudaSuccess || !p) {
             cudaGetLastError();
             return nullptr;
         }
-        unsigned zero = 0;
-        if (upload_sync(p, &zero, sizeof(zero)) != SCIR_OK) return nullptr;
-        g_err_word[dev] = p;
+        g_err_word[dev] = static_cast<unsigned*>(p);
     }
     return g_err_word[dev];
 }
@@ -296,6 +299,28 @@ SCIR_API int scir_release_scratch(void) {
     if (!pool) return SCIR_OK;
     SCIR_CUDA_TRY(cudaDeviceSynchronize());
     SCIR_CUDA_TRY(cudaMemPoolTrimTo(pool, 0));
+    return SCIR_OK;
+}
+
+SCIR_API int scir_scratch_usage(uint64_t* reserved, uint64_t* used) {
+    scir::clear_error();
+    if (!reserved || !used) return scir::set_error(SCIR_ERR_INVALID_ARG, "NULL output");
+    *reserved = *used = 0;
+    int dev = 0;
+    SCIR_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= scir::kMaxDevices)
+        return scir::set_error(SCIR_ERR_NO_DEVICE, "bad device %d", dev);
+    cudaMemPool_t pool = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(scir::g_pool_mu);
+        pool = scir::g_pool[dev];
+    }
+    if (!pool) return SCIR_OK;
+    cuuint64_t r = 0, u = 0;
+    SCIR_CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &r));
+    SCIR_CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &u));
+    *reserved = r;
+    *used = u;
     return SCIR_OK;
 }
 
