@@ -1,11 +1,14 @@
 #!/usr/bin/env python3
 """Throughput of the batched-filtering hot path on GB300.
 
-Default workload (N=1): polyphase resample_poly 160/147 of 256 channels x
-1,048,576 f32 N(0,1) samples with SciPy's default 3,201-tap Kaiser(5.0)
-design -- the configuration the headline metric (batched FIR Gsamples/s,
-chosen vs plain FP32) is quoted on.  Other configurations can be timed with
---workload (fir_short, fir_long, ragged, sosfilt, sosfiltfilt).
+Default workload (N=1): the long-tap batched FIR of 1,024 channels x 262,144
+f32 samples with a 4,095-tap Kaiser(8.6) band-pass -- the configuration the
+headline metric (batched FIR Gsamples/s, chosen BF16-split tensor-core form
+vs plain FP32 CUDA-core form at <= 1e-5 error) is quoted on.  The same line
+carries the plain-FP32 and BF16X3 timings of that workload and, under
+"resample_poly_160_147", the polyphase resample of 256 x 1,048,576 samples
+at 160/147 (HBM-bound).  Other configurations can be timed alone with
+--workload (resample, fir_short, ragged, sosfilt, sosfiltfilt).
 
 A step is one pass of the hot path over one batch of synthetic input,
 resident in HBM.  W warm-up steps, then K timed steps between a barrier and
@@ -14,11 +17,15 @@ stream, the max over ranks is reported by rank 0 as one JSON line.  Inputs
 are larger than L2 (129 MB) for the default workload.  `e2e` re-times the
 same work through the host-buffer C-ABI entry point (pinned host buffers,
 host<->device copies inside the timed region).  `cpu_baseline` times the CPU
-restatement of the reference's own algorithm on a bounded sample.
+restatement of the reference's own algorithm on a bounded sample, on all
+host cores and on one.
 
 --impl reference times the reference's CPU implementation of the path (the
-restated loops; the Rust reference cannot be compiled here) on the host cores
-with all threads.
+C restatement of its loops; the Rust reference cannot be compiled here or on
+the GPU machine) on the host cores, without loading this package.
+
+--probe-peaks prints the measured FP32 and FP64 FMA throughput of the GPU
+(the denominators of the CUDA-core-bound rooflines).
 
 Multi-GPU: torchrun, one rank per GPU; every rank processes its own full batch
 of channels (weak scaling, no data-path collective).
@@ -39,13 +46,6 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
-
-# FP32 FFMA throughput measured on this machine's GB300 with an independent-chain
-# FFMA loop (72.6 TFLOP/s); used only for CUDA-core-bound workloads.
-FP32_PEAK_TFLOPS = 72.6
-# FP64 DFMA throughput measured the same way (1.19 TFLOP/s, ~1/60 of FP32).
-FP64_PEAK_TFLOPS = 1.19
-
 
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -159,6 +159,13 @@ class Workload:
     bound = "hbm"
     launches_per_step = 1
     flush_l2 = False      # working set below L2: flush before every timed step
+    cpu_dtype = "f32"     # arithmetic of the restated reference loop
+
+    def host_release(self):
+        """Drops the pinned host buffers of the end-to-end leg."""
+        for a in ("hx", "hy", "hyv", "hyf", "hx_np", "hy_np", "htaps"):
+            if hasattr(self, a):
+                delattr(self, a)
 
     def products(self, precision=None):
         return 1
@@ -175,6 +182,7 @@ class Workload:
 class Resample(Workload):
     name = "resample_poly_160_147"
     B, N, UP, DOWN = 256, 1048576, 160, 147
+    cpu_dtype = "f64"
 
     def __init__(self, torch, dev, precision, channels=None):
         import scir_gb300 as S
@@ -241,19 +249,37 @@ class Resample(Workload):
         self.S.resample_poly_host(self.hx_np, self.UP, self.DOWN, precision=self.precision,
                                   out=self.hy_np)
 
-    # the reference's CPU algorithm (zero-stuff, full convolution, decimate)
+    # the reference's CPU algorithm (zero-stuff, full convolution, decimate,
+    # crates/scir-signal/src/lib.rs:313-362) generalised to 160/147 with the
+    # SciPy default design (the reference itself accepts only 2/3)
+    @classmethod
+    def cpu_taps(cls):
+        import scipy.signal as ss
+        mr = max(cls.UP, cls.DOWN)
+        return ss.firwin(2 * 10 * mr + 1, 1.0 / mr, window=("kaiser", 5.0)) * cls.UP
+
     def cpu_sample(self, O, threads, per_channel):
         rng = np.random.default_rng(1)
         x = rng.standard_normal((threads, per_channel))
-        h = self.S.resample_poly_default_taps(self.UP, self.DOWN)
+        h = self.cpu_taps()
         t0 = time.perf_counter()
         O.resample_poly_ref_f64(x, self.UP, self.DOWN, h)
         return threads * per_channel, time.perf_counter() - t0
 
-    def cpu_sample_desc(self, threads, per_channel):
-        return (f"{threads} channels x {per_channel} samples per step through the restated "
+    def cpu_row_len(self):
+        return self.N
+
+    def cpu_sample_desc(self, rows, per_channel):
+        return (f"{rows} channels x {per_channel} samples per step through the restated "
                 f"reference resample_poly (zero-stuff by 160, full 3,201-tap convolution, "
-                f"decimate by 147), f64, one OpenMP thread per channel")
+                f"decimate by 147), f64, channels spread over OpenMP threads")
+
+    def scipy_sample(self, per_channel):
+        import scipy.signal as ss
+        x = np.random.default_rng(1).standard_normal((1, per_channel))
+        t0 = time.perf_counter()
+        ss.resample_poly(x, self.UP, self.DOWN, axis=1)
+        return per_channel, time.perf_counter() - t0, "scipy.signal.resample_poly (polyphase, f64)"
 
 
 class FirLong(Workload):
@@ -350,19 +376,40 @@ class FirLong(Workload):
         self.S.fir_batched_host(self.hx.numpy(), self.htaps, self.S.FirMode.LFILTER,
                                 self.precision, out=self.hy.numpy())
 
-    # the reference's CPU loop (crates/scir-gpu/src/lib.rs:1134-1152), f32
-    def cpu_sample(self, O, threads, per_channel):
+    # the reference's CPU loop (crates/scir-gpu/src/lib.rs:1134-1152), f32, on
+    # rows of the configuration's signal with its band-pass taps
+    @classmethod
+    def cpu_inputs(cls, rows, per_channel):
+        import scipy.signal as ss
         rng = np.random.default_rng(1)
-        x = rng.uniform(-1, 1, (threads, per_channel)).astype(np.float32)
-        taps = np.ones(self.K, np.float32) / self.K
+        t = np.arange(per_channel)
+        x = rng.standard_normal((rows, per_channel)) * 0.1
+        for r in range(rows):
+            f, ph = rng.uniform(0, 0.5, 32), rng.uniform(0, 2 * np.pi, 32)
+            x[r] += np.sin(2 * np.pi * np.outer(f, t) + ph[:, None]).sum(0) / 32
+        taps = ss.firwin(cls.K, [0.1, 0.3], window=("kaiser", 8.6), pass_zero=False)
+        return x.astype(np.float32), taps.astype(np.float32)
+
+    def cpu_sample(self, O, threads, per_channel):
+        x, taps = self.cpu_inputs(threads, per_channel)
         t0 = time.perf_counter()
         O.fir1d_batched_f32(x, taps)
         return threads * per_channel, time.perf_counter() - t0
 
-    def cpu_sample_desc(self, threads, per_channel):
-        return (f"{threads} channels x {per_channel} samples per step through the restated "
-                f"reference fir1d_batched_f32 loop (4,095 taps, f32, sequential), one OpenMP "
-                f"thread per channel")
+    def cpu_row_len(self):
+        return self.N
+
+    def cpu_sample_desc(self, rows, per_channel):
+        return (f"{rows} channels x {per_channel} samples per step through the restated "
+                f"reference fir1d_batched_f32 loop (4,095 taps, f32, sequential per channel), "
+                f"channels spread over OpenMP threads")
+
+    def scipy_sample(self, per_channel):
+        import scipy.signal as ss
+        x, taps = self.cpu_inputs(1, per_channel)
+        t0 = time.perf_counter()
+        ss.lfilter(taps.astype(np.float64), 1.0, x[0].astype(np.float64))
+        return per_channel, time.perf_counter() - t0, "scipy.signal.lfilter (direct form, f64)"
 
 
 class FirShort(Workload):
@@ -452,9 +499,20 @@ class FirShort(Workload):
         O.fir1d_batched_f32(x, taps)
         return threads * per_channel, time.perf_counter() - t0
 
-    def cpu_sample_desc(self, threads, per_channel):
-        return (f"{threads} channels x {per_channel} samples per step through the restated "
-                f"reference fir1d_batched_f32 loop (63 taps, f32), one OpenMP thread per channel")
+    def cpu_row_len(self):
+        return self.N
+
+    def cpu_sample_desc(self, rows, per_channel):
+        return (f"{rows} channels x {per_channel} samples per step through the restated "
+                f"reference fir1d_batched_f32 loop (63 taps, f32), channels spread over OpenMP "
+                f"threads")
+
+    def scipy_sample(self, per_channel):
+        import scipy.signal as ss
+        x = np.random.default_rng(1).uniform(-1, 1, per_channel)
+        t0 = time.perf_counter()
+        ss.lfilter(ss.firwin(self.K, 0.2, window="hamming"), 1.0, x)
+        return per_channel, time.perf_counter() - t0, "scipy.signal.lfilter (direct form, f64)"
 
 
 class Ragged(Workload):
@@ -471,17 +529,23 @@ class Ragged(Workload):
         self.S, self.torch, self.dev = S, torch, dev
         self.precision = S.Precision.FP32 if precision == S.Precision.AUTO else precision
         count = channels or self.COUNT
-        rng = np.random.default_rng(1)
-        self.n = np.exp(rng.uniform(np.log(1024), np.log(4194304), count)).round().astype(np.int64)
-        self.k = np.exp(rng.uniform(np.log(16), np.log(2048), count)).round().astype(np.int64)
-        cut = rng.uniform(0.05, 0.45, count)
+        self.n, self.k, cut = self.draw(count)
         taps = np.concatenate([ss.firwin(int(k), c, window="hamming") for k, c in zip(self.k, cut)])
         self.taps = torch.from_numpy(taps.astype(np.float32)).to(dev)
         g = torch.Generator(device=dev).manual_seed(0)
         self.x = torch.rand(int(self.n.sum()), device=dev, generator=g) * 2 - 1
         self.plan = S.RaggedPlan(self.n, self.k, S.FirMode.LFILTER, self.precision)
         self.y = torch.empty(self.plan.y_len, device=dev)
-        self.kernel = "ragged_kernel"
+        self.kernel = "ragged_kernel (one persistent launch, replayed from a CUDA graph)"
+        self.graph = None
+
+    @staticmethod
+    def draw(count):
+        """Signal lengths, tap counts and cutoffs of the ragged set (seeded)."""
+        rng = np.random.default_rng(1)
+        n = np.exp(rng.uniform(np.log(1024), np.log(4194304), count)).round().astype(np.int64)
+        k = np.exp(rng.uniform(np.log(16), np.log(2048), count)).round().astype(np.int64)
+        return n, k, rng.uniform(0.05, 0.45, count)
 
     @classmethod
     def config(cls):
@@ -498,8 +562,24 @@ class Ragged(Workload):
     def alg_flops(self):
         return 2.0 * self.plan.macs
 
+    def prepare(self):
+        """Records the plan's launch (work-counter reset + persistent kernel)
+        into a CUDA graph once; every step replays it.  Runs after the
+        autotuner, which rebuilds the plan's tile table."""
+        self.S.init(self.dev.index or 0)
+        self.plan.run(self.x, self.taps, self.y)
+        self.torch.cuda.synchronize()
+        cs = self.torch.cuda.Stream(self.dev)
+        self.graph = self.S.GraphCapture(cs)
+        with self.graph:
+            self.plan.run(self.x, self.taps, self.y, stream=cs)
+        self.torch.cuda.synchronize()
+
     def step(self, stream, precision=None):
-        self.plan.run(self.x, self.taps, self.y, stream=stream)
+        if self.graph is not None:
+            self.graph.launch(stream)
+        else:
+            self.plan.run(self.x, self.taps, self.y, stream=stream)
 
     def autotune(self):
         thr, ms = self.plan.autotune(self.x, self.taps, self.y)
@@ -543,14 +623,27 @@ class Ragged(Workload):
     def cpu_sample(self, O, threads, per_channel):
         rng = np.random.default_rng(1)
         x = rng.uniform(-1, 1, (threads, per_channel)).astype(np.float32)
-        taps = np.ones(int(np.median(self.k)), np.float32)
+        taps = np.ones(self.median_k(), np.float32)
         t0 = time.perf_counter()
         O.fir1d_batched_f32(x, taps)
         return threads * per_channel, time.perf_counter() - t0
 
-    def cpu_sample_desc(self, threads, per_channel):
-        return (f"{threads} signals x {per_channel} samples per step through the restated "
-                f"reference fir1d_batched_f32 loop at the median tap count")
+    def median_k(self):
+        return int(np.median(self.draw(self.COUNT)[1]))
+
+    def cpu_row_len(self):
+        return 1 << 19  # about the mean signal length (504 k)
+
+    def cpu_sample_desc(self, rows, per_channel):
+        return (f"{rows} signals x {per_channel} samples per step through the restated "
+                f"reference fir1d_batched_f32 loop at the median tap count ({self.median_k()})")
+
+    def scipy_sample(self, per_channel):
+        import scipy.signal as ss
+        x = np.random.default_rng(1).uniform(-1, 1, per_channel)
+        t0 = time.perf_counter()
+        ss.lfilter(ss.firwin(self.median_k(), 0.25, window="hamming"), 1.0, x)
+        return per_channel, time.perf_counter() - t0, "scipy.signal.lfilter at the median tap count"
 
 
 class Sos(Workload):
@@ -558,6 +651,7 @@ class Sos(Workload):
     as 8 sections; sosfilt (or sosfiltfilt with odd padding and zi)."""
     name = "sosfilt_16384"
     B, N = 16384, 131072
+    cpu_dtype = "f64"
     bound = "hbm"
     filtfilt = False
 
@@ -577,7 +671,7 @@ class Sos(Workload):
         self.precision = precision
         if channels:
             self.B = channels
-        self.sos = ss.butter(8, [0.001, 0.002], btype="bandpass", output="sos")
+        self.sos = self.cpu_sos()
         g = torch.Generator(device=dev).manual_seed(0)
         self.x = torch.randn((self.B, self.N), device=dev, generator=g)
         self.y = torch.empty_like(self.x)
@@ -627,18 +721,39 @@ class Sos(Workload):
     def host_step(self):
         self.step(None)
 
+    @staticmethod
+    def cpu_sos():
+        import scipy.signal as ss
+        return ss.butter(8, [0.001, 0.002], btype="bandpass", output="sos")
+
     def cpu_sample(self, O, threads, per_channel):
         rng = np.random.default_rng(1)
         x = rng.standard_normal((threads, per_channel))
+        sos = self.cpu_sos()
         t0 = time.perf_counter()
         if self.filtfilt:
-            O.filtfilt_ref_f64(self.sos, x)
+            O.filtfilt_ref_f64(sos, x)
         else:
-            O.sosfilt_f64(self.sos, x)
+            O.sosfilt_f64(sos, x)
         return threads * per_channel, time.perf_counter() - t0
 
-    def cpu_sample_desc(self, threads, per_channel):
-        return (f"{threads} channels x {per_channel} samples per step through the restated "
+    def scipy_sample(self, per_channel):
+        import scipy.signal as ss
+        x = np.random.default_rng(1).standard_normal(per_channel)
+        sos = self.cpu_sos()
+        t0 = time.perf_counter()
+        if self.filtfilt:
+            ss.sosfiltfilt(sos, x)
+        else:
+            ss.sosfilt(sos, x)
+        return per_channel, time.perf_counter() - t0, (
+            "scipy.signal." + ("sosfiltfilt (odd pad, zi)" if self.filtfilt else "sosfilt") + ", f64")
+
+    def cpu_row_len(self):
+        return self.N
+
+    def cpu_sample_desc(self, rows, per_channel):
+        return (f"{rows} channels x {per_channel} samples per step through the restated "
                 f"reference DF2T {'filtfilt' if self.filtfilt else 'sosfilt'} (f64)")
 
 
@@ -670,17 +785,63 @@ def smi_index(local_rank: int) -> int:
 
 
 def calibrate_cpu(W, O, threads, target_s):
-    per = 64
+    """A bounded sample of the workload that takes about target_s on
+    `threads` host threads: (rows, samples per row).  Rows grow to the
+    configuration's own length first, then more rows (a multiple of the
+    thread count) are taken."""
+    full = W.cpu_row_len()
+    rows, per = threads, 64
     while True:
-        n, dt = W.cpu_sample(O, threads, per)
-        if dt >= 0.25 or per >= 1 << 22:
+        n, dt = W.cpu_sample(O, rows, per)
+        if dt >= 0.25 or per >= full:
+            break
+        per = min(full, per * 4)
+    scale = target_s / max(dt, 1e-6)
+    if per < full and scale > 1:
+        per2 = min(full, int(per * scale))
+        scale /= per2 / per
+        per = per2
+    if per >= full:
+        rows = max(threads, int(round(rows * scale / threads)) * threads)
+    else:
+        per = max(16, int(per * scale))
+    return rows, per
+
+
+def cpu_rates(W, O, threads, target_s, reps):
+    """Rate of the restated reference loop on `threads` host threads, over
+    `reps` bounded samples of ~target_s each: (Gsamples/s, sample text,
+    seconds per sample)."""
+    O.set_threads(threads)
+    rows, per = calibrate_cpu(W, O, threads, target_s)
+    tot_n, tot_t = 0, 0.0
+    for _ in range(reps):
+        n, dt = W.cpu_sample(O, rows, per)
+        tot_n += n
+        tot_t += dt
+    return (tot_n / tot_t / 1e9, W.cpu_sample_desc(rows, per) + f", {threads} host thread(s)",
+            tot_t / reps)
+
+
+def scipy_rate(W, target_s=2.0):
+    """SciPy's FP64 implementation of the same operation on one host core, a
+    secondary CPU reference."""
+    per = 4096
+    while True:
+        n, dt, what = W.scipy_sample(per)
+        if dt >= 0.25 or per >= 1 << 24:
             break
         per *= 4
-    per = max(16, int(per * target_s / max(dt, 1e-6)))
-    return per
+    per = max(1024, int(per * target_s / max(dt, 1e-6)))
+    n, dt, what = W.scipy_sample(per)
+    return {"value": n / dt / 1e9, "unit": W.unit, "cores": 1,
+            "sample": f"1 channel x {per} samples through {what}"}
 
 
 def run_reference(args):
+    """The reference arm: the C restatement of the reference's CPU loop for
+    the workload (oracle/), timed on the host cores.  This package is never
+    imported here, so no kernel library of this repository is loaded."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
@@ -690,32 +851,96 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     O.set_threads(threads)
     W = WORKLOADS[args.workload].__new__(WORKLOADS[args.workload])
-    import scir_gb300 as S
-    W.S = S
     per_step_s = max(0.5, min(3.0, 90.0 / max(1, args.steps + args.warmup)))
-    per = calibrate_cpu(W, O, threads, per_step_s)
+    rows, per = calibrate_cpu(W, O, threads, per_step_s)
     for _ in range(args.warmup):
-        W.cpu_sample(O, threads, per)
+        W.cpu_sample(O, rows, per)
     total_n, total_t = 0, 0.0
     for _ in range(args.steps):
-        n, dt = W.cpu_sample(O, threads, per)
+        n, dt = W.cpu_sample(O, rows, per)
         total_n += n
         total_t += dt
     value = total_n / total_t / 1e9
+    one, one_desc, _ = cpu_rates(W, O, 1, 3.0, 1)
     cfg = WORKLOADS[args.workload].config()
     line = {"impl": "reference", "metric": W.metric, "value": value, "unit": W.unit,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000 * total_t / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": W.cpu_dtype, "data": "synthetic",
             "config": cfg,
             "cpu_baseline": {"value": value, "unit": W.unit, "cores": threads, "kind": "port",
-                             "sample": W.cpu_sample_desc(threads, per)},
+                             "sample": W.cpu_sample_desc(rows, per) + f", {threads} host threads"},
+            "single_core": {"value": one, "unit": W.unit, "cores": 1, "sample": one_desc},
+            "scipy": scipy_rate(W),
             "e2e": {"value": value, "unit": W.unit, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "note": "the reference is Rust and no Rust toolchain exists here or on the GPU box; "
-                    "this arm times the C restatement of its CPU loop"}
+                    "this arm times the C restatement of its CPU loop (oracle/scir_oracle.c) "
+                    "on a bounded sample of the configuration per step, on all host threads; "
+                    "single_core is the same loop on one thread (the reference is "
+                    "single-threaded); scipy is SciPy's FP64 implementation on one core"}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def time_steps(torch, W, stream, steps, precision=None, flush=None):
+    """Per-step milliseconds of `steps` steps, CUDA events on the launch stream."""
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for i in range(steps):
+        if flush is not None:
+            flush.fill_(float(i))  # 256 MB write evicts L2 (129 MB) between steps
+        ev0[i].record(stream)
+        W.step(stream, precision)
+        ev1[i].record(stream)
+    torch.cuda.synchronize()
+    return [ev0[i].elapsed_time(ev1[i]) for i in range(steps)]
+
+
+def roofline(W, kern_ms, peaks, fma):
+    """Roofline of the dominant kernel: the algorithmic work of one launch
+    over its mean duration, against the binding peak."""
+    rl = getattr(W, "roofline_launches", W.launches_per_step)
+    if W.bound == "hbm":
+        achieved = W.alg_bytes() / rl / (kern_ms / 1e3) / 1e9
+        peak, unit, src = peaks["hbm_gbs"], "GB/s", peaks["source"]
+    elif W.bound == "tensor" and W.products() > 1:
+        achieved = W.alg_flops() / rl / (kern_ms / 1e3) / 1e12
+        peak, unit, src = peaks["bf16_tflops"], "TFLOP/s", peaks["source"]
+    else:
+        fp64 = W.bound == "fp64"
+        achieved = W.alg_flops() / rl / (kern_ms / 1e3) / 1e12
+        peak, unit = fma(fp64), "TFLOP/s"
+        src = "measured live by scir_probe_fma_peak (" + ("FP64 DFMA" if fp64 else "FP32 FFMA") + ")"
+    return {"bound": W.bound, "achieved": achieved, "peak": peak, "unit": unit,
+            "frac": achieved / peak, "traffic": profile_traffic(W.name), "kernel": W.kernel,
+            "kernel_ms": kern_ms, "peak_source": src}
+
+
+def resample_record(torch, S, dev, stream, steps, peaks, fma):
+    """The polyphase resample configuration (256 x 1,048,576, 160/147) as a
+    sub-record of the default line: device rate, HBM roofline, error, and the
+    tensor-core (BF16X3) form beside the chosen one."""
+    W = Resample(torch, dev, S.Precision.AUTO)
+    tuned = W.autotune()
+    for _ in range(3):
+        W.step(stream)
+    per = time_steps(torch, W, stream, steps)
+    ms = statistics.mean(per)
+    rec = {"workload": Resample.config()["workload"], "precision": "AUTO", "autotune": tuned,
+           "value": W.samples_per_step() / (ms / 1e3) / 1e9, "unit": W.unit, "ms_per_step": ms,
+           "roofline": roofline(W, ms, peaks, fma), "max_rel_err_vs_fp64": W.max_rel_err(),
+           "gpu_launches": W.launches_per_step * steps}
+    for _ in range(3):
+        W.step(stream, S.Precision.BF16X3)
+    tc = statistics.mean(time_steps(torch, W, stream, steps, S.Precision.BF16X3))
+    rec["bf16x3"] = {"ms_per_step": tc, "value": W.samples_per_step() / (tc / 1e3) / 1e9,
+                     "max_rel_err_vs_fp64": W.max_rel_err(S.Precision.BF16X3),
+                     "kernel": "poly_tc_kernel (tensor cores) + tap-operand build"}
+    del W
+    torch.cuda.empty_cache()
+    return rec
 
 
 def run_ours(args):
@@ -730,6 +955,13 @@ def run_ours(args):
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
     peaks = load_peaks()
+    fma_cache = {}
+
+    def fma(fp64):
+        if fp64 not in fma_cache:
+            fma_cache[fp64] = S.probe_fma_peak(fp64)
+        return fma_cache[fp64]
+
     if args.precision in S.Precision.__members__:
         prec = S.Precision[args.precision]
     elif args.workload in ("sosfilt", "sosfiltfilt") and args.precision in S.SosPrecision.__members__:
@@ -744,25 +976,17 @@ def run_ours(args):
             dist.barrier(device_ids=[local])
 
     tuned = None if args.no_autotune else W.autotune()
+    if hasattr(W, "prepare"):
+        W.prepare()
     for _ in range(max(3, args.warmup)):
         W.step(stream)
     torch.cuda.synchronize()
     barrier()
     torch.cuda.synchronize()
     flush = torch.empty(64 << 20, dtype=torch.float32, device=dev) if W.flush_l2 else None
-    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     with ClockSampler(smi_index(local)) as clk:
-        torch.cuda.synchronize()
-        for i in range(args.steps):
-            if flush is not None:
-                flush.fill_(float(i))  # 256 MB write evicts L2 (129 MB) between steps
-            ev0[i].record(stream)
-            W.step(stream)
-            ev1[i].record(stream)
-        torch.cuda.synchronize()
+        per_step = time_steps(torch, W, stream, args.steps, flush=flush)
     barrier()
-    per_step = [ev0[i].elapsed_time(ev1[i]) for i in range(args.steps)]
     total_ms = sum(per_step)
     t = torch.tensor([total_ms], device=dev)
     if world > 1:
@@ -776,17 +1000,22 @@ def run_ours(args):
     if prec != S.Precision.FP32:
         for _ in range(3):
             W.step(stream, S.Precision.FP32)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
-            W.step(stream, S.Precision.FP32)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        pms = e0.elapsed_time(e1) / args.steps
+        pms = statistics.mean(time_steps(torch, W, stream, args.steps, S.Precision.FP32,
+                                         flush=flush))
         plain = {"value": W.samples_per_step() / (pms / 1e3) / 1e9, "unit": W.unit,
-                 "ms_per_step": pms}
+                 "ms_per_step": pms, "max_rel_err_vs_fp64": W.max_rel_err(S.Precision.FP32),
+                 "chosen_speedup": pms / ms_step}
     err = W.max_rel_err()
+    # the two-product split beside the chosen form of the tensor-core FIR
+    bf16x3 = None
+    if isinstance(W, FirLong) and prec not in (S.Precision.BF16X3, S.Precision.FP32,
+                                               S.Precision.REF_EXACT):
+        for _ in range(3):
+            W.step(stream, S.Precision.BF16X3)
+        xms = statistics.mean(time_steps(torch, W, stream, args.steps, S.Precision.BF16X3))
+        bf16x3 = {"ms_per_step": xms, "value": W.samples_per_step() / (xms / 1e3) / 1e9,
+                  "max_rel_err_vs_fp64": W.max_rel_err(S.Precision.BF16X3),
+                  "vs_plain_fp32": (plain["ms_per_step"] / xms) if plain else None}
 
     # end to end through the host-buffer C-ABI call
     h2d, d2h = W.host_setup()
@@ -805,43 +1034,27 @@ def run_ours(args):
     e2e = {"value": e2e_value, "unit": W.unit, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h} if (h2d or d2h) else None
 
-    # roofline of the dominant kernel: algorithmic work of one launch over the
-    # mean launch duration (a step of rl launches of the same kernel does rl
-    # launches' worth of the step's algorithmic bytes / flops)
-    rl = getattr(W, "roofline_launches", W.launches_per_step)
-    kern_ms = statistics.mean(per_step) / rl
-    if W.bound == "hbm":
-        achieved = W.alg_bytes() / rl / (kern_ms / 1e3) / 1e9
-        peak, unit = peaks["hbm_gbs"], "GB/s"
-    elif W.bound == "fp64":
-        achieved = W.alg_flops() / rl / (kern_ms / 1e3) / 1e12
-        peak, unit = FP64_PEAK_TFLOPS, "TFLOP/s"
-    elif W.bound == "tensor" and W.products() > 1:
-        achieved = W.alg_flops() / rl / (kern_ms / 1e3) / 1e12
-        peak, unit = peaks["bf16_tflops"], "TFLOP/s"
-    else:
-        achieved = W.alg_flops() / rl / (kern_ms / 1e3) / 1e12
-        peak, unit = FP32_PEAK_TFLOPS, "TFLOP/s"
-    traffic = profile_traffic(W.name)
+    kern_ms = statistics.mean(per_step) / getattr(W, "roofline_launches", W.launches_per_step)
+    roof = roofline(W, kern_ms, peaks, fma)
     per_signal = None
     if hasattr(W, "per_signal_ms"):
         W.per_signal_ms(stream)  # warm
         per_signal = {"ms_per_step": W.per_signal_ms(stream),
                       "note": "the same signals, one scir_fir_batched_f32 launch each"}
+    W.host_release()
+
+    extra = None
+    if args.workload == DEFAULT_WORKLOAD and not args.no_extra and args.channels is None:
+        extra = resample_record(torch, S, dev, stream, args.steps, peaks, fma)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         import oracle as O
         threads = os.cpu_count() or 1
-        O.set_threads(threads)
-        per = calibrate_cpu(W, O, threads, 3.0)
-        tot_n, tot_t = 0, 0.0
-        for _ in range(3):
-            n, dt = W.cpu_sample(O, threads, per)
-            tot_n += n
-            tot_t += dt
-        cpu = {"value": tot_n / tot_t / 1e9, "unit": W.unit, "cores": threads, "kind": "port",
-               "sample": W.cpu_sample_desc(threads, per)}
+        v, desc, _ = cpu_rates(W, O, threads, 3.0, 3)
+        v1, desc1, _ = cpu_rates(W, O, 1, 3.0, 1)
+        cpu = {"value": v, "unit": W.unit, "cores": threads, "kind": "port", "sample": desc,
+               "single_core": {"value": v1, "cores": 1, "sample": desc1}}
     clocks = clk.summary()
     if world > 1:
         dist.destroy_process_group()
@@ -851,21 +1064,34 @@ def run_ours(args):
         "metric": W.metric, "value": value, "unit": W.unit, "n_gpus": world,
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded torch.randn on the device)",
+        "data": "synthetic (seeded torch generators on the device)",
         "config": run_config(W, prec, world),
-        "roofline": {"bound": W.bound, "achieved": achieved, "peak": peak, "unit": unit,
-                     "frac": achieved / peak, "traffic": traffic,
-                     "kernel": W.kernel, "kernel_ms": kern_ms,
-                     "peak_source": peaks["source"] if W.bound == "hbm" else "probe"},
+        "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": W.launches_per_step * args.steps,
         "autotune": tuned,
         "max_rel_err_vs_fp64": err,
         "plain_fp32": plain,
+        "bf16x3": bf16x3,
         "per_signal_launches": per_signal,
         "clocks": clocks,
     }
+    if extra is not None:
+        line["resample_poly_160_147"] = extra
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_probe():
+    import torch
+
+    import scir_gb300 as S
+    torch.cuda.set_device(0)
+    line = {"probe": "FMA throughput of the CUDA cores (scir_probe_fma_peak)",
+            "fp32_tflops": [S.probe_fma_peak(False) for _ in range(3)],
+            "fp64_tflops": [S.probe_fma_peak(True) for _ in range(3)],
+            "device": torch.cuda.get_device_name(0)}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -881,20 +1107,29 @@ def run_config(W, prec, world):
     return cfg
 
 
+DEFAULT_WORKLOAD = "fir_long"
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="resample")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--precision", default="AUTO")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the resample sub-record of the default workload")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the library autotuner (default dispatch heuristics)")
     ap.add_argument("--channels", type=int, default=None,
                     help="override the channel count (profiling runs on a smaller case)")
+    ap.add_argument("--probe-peaks", action="store_true",
+                    help="print the measured FP32/FP64 FMA throughput and exit")
     args = ap.parse_args()
+    if args.probe_peaks:
+        return run_probe()
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

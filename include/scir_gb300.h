@@ -141,6 +141,12 @@ SCIR_API int scir_device_count(int* count);
  * since the last call.  Synchronises with the device.  The reference has no
  * device-side failure reporting (its CUDA path cannot run at all). */
 SCIR_API int scir_device_errors(unsigned* code);
+/* Measured FMA throughput of the current device's CUDA cores in TFLOP/s
+ * (fp64 = 0: FP32 FFMA, 1: FP64 DFMA): independent FMA chains at full
+ * occupancy, timed with CUDA events (synchronous, ~0.3 s).  The roofline
+ * denominator of FP32- and FP64-pipe-bound kernels.  No reference
+ * counterpart. */
+SCIR_API int scir_probe_fma_peak(int fp64, double* tflops);
 /* Self-test of the bounded-wait failure path on the current device (no
  * reference counterpart: the reference has no device-side failure
  * reporting).  A two-warp pipeline copies n_chunks chunks of 1,024 floats

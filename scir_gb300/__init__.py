@@ -325,6 +325,13 @@ def release_scratch() -> None:
     _check(load().scir_release_scratch())
 
 
+def probe_fma_peak(fp64: bool = False) -> float:
+    """Measured FP32 (or FP64) FMA throughput of the current device, TFLOP/s."""
+    v = ctypes.c_double(0.0)
+    _check(load().scir_probe_fma_peak(1 if fp64 else 0, ctypes.byref(v)))
+    return float(v.value)
+
+
 def scratch_usage() -> tuple:
     """(reserved, used) bytes of the library's scratch pool on the current
     device; (0, 0) before any call needed scratch."""

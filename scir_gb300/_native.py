@@ -26,6 +26,7 @@ SIGNATURES = {
     "scir_device_count": (_int, [ctypes.POINTER(_int)]),
     "scir_device_errors": (_int, [ctypes.POINTER(ctypes.c_uint)]),
     "scir_release_scratch": (_int, []),
+    "scir_probe_fma_peak": (_int, [_int, ctypes.POINTER(ctypes.c_double)]),
     "scir_selftest_pipeline": (_int, [_vp, _i64, _i64, ctypes.c_longlong, _vp, _vp]),
     "scir_scratch_usage": (_int, [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "scir_fir_out_len": (_i64, [_i64, _i64, _int]),
