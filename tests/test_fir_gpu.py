@@ -173,6 +173,25 @@ def test_tensor_core_cfg3_bandpass(cuda):
         assert normwise_err(y[rows], ref) < 1e-5, prec
 
 
+@pytest.mark.parametrize("prec", [S.Precision.BF16X3, S.Precision.BF16X6])
+@pytest.mark.parametrize("k", [2, 3, 16, 17, 64, 1025])
+def test_tensor_core_unaligned_rows(cuda, prec, k):
+    # x starting one float past a 16-byte boundary (scalar signal loads), an
+    # odd output row stride (scalar stores), 260 channels (a partial third
+    # channel group) and 2,500 samples (a partial third output window)
+    import torch
+    rng = np.random.default_rng(k)
+    big = rng.uniform(-1, 1, (260, 2502)).astype(np.float32)
+    taps = (rng.standard_normal(k) / np.sqrt(k)).astype(np.float32)
+    xd = _dev(big, cuda)[:, 1:2501]
+    out = torch.zeros((260, 2503), device=cuda)[:, :2500]
+    ref = O.fir_mode_f64(big[:, 1:2501].astype(np.float64), taps.astype(np.float64),
+                         int(S.FirMode.LFILTER))
+    S.fir_batched(xd, _dev(taps, cuda), S.FirMode.LFILTER, prec, out=out)
+    tol = TOL_FP32 if prec == S.Precision.BF16X6 else TOL_BF16X3
+    assert normwise_err(out.cpu().numpy(), ref) < tol
+
+
 def test_tensor_core_strided_and_repeat(cuda):
     import torch
     rng = np.random.default_rng(21)
