@@ -5,12 +5,18 @@
 // channels that is 512 warps, under one per scheduler, and each warp then
 // runs every section of every sample alone (measured on GB300: the time of a
 // 2,048-channel launch equals that of a 16,384-channel one).  Here a CTA of
-// G warps owns 32 channels and warp w owns sections [w*SPW, (w+1)*SPW): a
-// tile of 32 channels x 32 samples moves through the warps in place in a
+// G warps owns 64 channels and warp w owns sections [w*SPW, (w+1)*SPW): a
+// tile of 64 channels x 32 samples moves through the warps in place in a
 // shared-memory ring, so the G warps filter G different tiles at once and
-// every scheduler gets several warps.
-//
-// Ring protocol (kRing slots, slot r holds global tile g with g % kRing = r):
+// every scheduler gets several warps.  Lane l carries channels l and l + 32
+// as the two halves of packed f32x2 operations: every packed FMA applies one
+// section to two independent channels, so each warp has two independent
+// recursions per lane to interleave (the coefficients are duplicated in both
+// halves of their register pairs).  Each half performs exactly the scalar
+// section update's operations in the same order, so the results equal those
+// of one thread per channel bit for bit.
+
+// Ring protocol (kRing = G + 4 slots, slot r holds global tile g with g % kRing = r):
 //   warp 0 loads tile g + kAhead (cp.async, or computed extension samples)
 //   once the last warp has released the slot (tile g + kAhead - kRing),
 //   then filters tile g with its sections and arrives on done[0][r];
@@ -42,16 +48,20 @@
 namespace scir {
 namespace {
 
-// kTT (32, from sos_math.cuh): channels per CTA = samples per tile
-constexpr int kRing = 8;    // tile slots
+// kTT (32, from sos_math.cuh): samples per tile = lanes
+constexpr int kCH = 2 * kTT;  // channels per CTA: lane l owns rows l and l + 32
 constexpr int kLd = kTT + 1;
 
 template <int NS>
 struct PipeShape {
-    static constexpr int G = NS < 4 ? NS : 4;  // warps
+    // warps: up to 4 sections per warp (the duplicated coefficient pairs of
+    // 4 sections take 48 registers)
+    static constexpr int G = NS < 4 ? NS : NS <= 12 ? 4 : 8;
     static constexpr int SPW = NS / G;         // sections per warp
+    static constexpr int kRing = G + 4;        // tile slots
     static constexpr int kAhead = kRing - G;   // tiles loaded ahead of warp 0
     static_assert(NS % G == 0, "section count must divide over the warps");
+    static_assert(SPW <= 4, "at most 4 sections per warp");
 };
 
 __device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
@@ -71,15 +81,14 @@ __device__ __forceinline__ void cp_async_wait() {
 enum StreamKind { kSos = 0, kFwd = 1, kBwd = 2 };
 
 // The coefficients of a warp's sections (fixed for the launch) live in
-// registers as the halves of packed pairs: section 2i in .x, 2i+1 in .y.
-// A coupled half holds sigma-1, omega, -omega, C1, C2, b0; a DF2T half
-// holds b0, b1, b2, -a1, -a2.  The negated values are exact.
-struct PairSec {
+// registers, each duplicated in both halves of a pair (one section, two
+// channels).  A coupled section holds sigma-1, omega, -omega, C1, C2, b0; a
+// DF2T section holds b0, b1, b2, -a1, -a2.  The negated values are exact.
+struct PackSec {
     float2 f[6];
 };
 
-__device__ __forceinline__ void put_sec(PairSec& p, int half, const SosCoef& sc, int s,
-                                        bool coupled) {
+__device__ __forceinline__ void put_sec(PackSec& p, const SosCoef& sc, int s, bool coupled) {
     float v[6];
     if (coupled) {
         v[0] = sc.cp[s][0];
@@ -97,43 +106,17 @@ __device__ __forceinline__ void put_sec(PairSec& p, int half, const SosCoef& sc,
         v[5] = 0.0f;
     }
 #pragma unroll
-    for (int j = 0; j < 6; ++j) {
-        if (half == 0) p.f[j].x = v[j];
-        else p.f[j].y = v[j];
-    }
+    for (int j = 0; j < 6; ++j) p.f[j] = make_float2(v[j], v[j]);
 }
 
-// The arithmetic of sos_sec (PREC 2 / 3) for one section, on half H of its
-// pair.  FORM: 0 = FP32 DF2T, 1 = coupled, 2 = chosen per section (a warp
-// whose sections mix real and complex poles).
-template <int FORM, int H>
-__device__ __forceinline__ float sec_step(const PairSec& r, bool coupled, float& s1, float& s2,
-                                          float prev) {
-    auto c = [&](int j) { return H == 0 ? r.f[j].x : r.f[j].y; };
-    float out;
-    if (FORM == 1 || (FORM == 2 && coupled)) {
-        const float u = s1, v = s2;
-        out = fmaf(c(3), u, fmaf(c(4), v, c(5) * prev));
-        s1 = u + fmaf(c(0), u, fmaf(c(2), v, prev));
-        s2 = v + fmaf(c(1), u, c(0) * v);
-    } else {
-        out = fmaf(c(0), prev, s1);
-        s1 = fmaf(c(3), out, fmaf(c(1), prev, s2));
-        s2 = fmaf(c(4), out, c(2) * prev);
-    }
-    return out;
-}
-
-// Two sections of a warp run one sample apart in one packed (f32x2) step:
-// the first section at sample p (x = input) and the second at sample p - 1
-// (x = the first section's previous output).  Each half performs exactly the
-// operations of sec_step in the same order (fma.rn / mul.rn / add.rn per
-// element), so the outputs are bit-identical to the scalar cascade with half
-// the instructions.  S1 / S2 hold (s1, s2) of the two sections; FORM 0 or 1.
-template <int FORM>
-__device__ __forceinline__ float2 pair_step(const PairSec& r, float2& S1, float2& S2, float2 X) {
+// One section on two channels (the halves).  Coupled (COUPLED = true):
+//   out = C1*u + C2*v + b0*x;  u += (sigma-1)*u - omega*v + x;  v += omega*u + (sigma-1)*v
+// DF2T: out = b0*x + s1;  s1 = b1*x - a1*out + s2;  s2 = b2*x - a2*out.
+// Each half rounds exactly like the scalar fmaf / mul / add sequence.
+template <bool COUPLED>
+__device__ __forceinline__ float2 pack_step(const PackSec& r, float2& S1, float2& S2, float2 X) {
     float2 Y;
-    if (FORM == 1) {
+    if (COUPLED) {
         const float2 U = S1, V = S2;
         Y = __ffma2_rn(r.f[3], U, __ffma2_rn(r.f[4], V, __fmul2_rn(r.f[5], X)));
         S1 = __fadd2_rn(U, __ffma2_rn(r.f[0], U, __ffma2_rn(r.f[2], V, X)));
@@ -160,18 +143,20 @@ struct PipeArgs {
 };
 
 template <int NS, int PREC, bool FF>
-__global__ void __launch_bounds__(32 * PipeShape<NS>::G, 4)
+__global__ void __launch_bounds__(32 * PipeShape<NS>::G, 2)
 sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
-    constexpr int G = PipeShape<NS>::G, SPW = PipeShape<NS>::SPW, kAhead = PipeShape<NS>::kAhead;
-    __shared__ float tiles[kRing][kTT][kLd];  // [slot][row = channel][time]
+    constexpr int G = PipeShape<NS>::G, SPW = PipeShape<NS>::SPW;
+    constexpr int kRing = PipeShape<NS>::kRing, kAhead = PipeShape<NS>::kAhead;
+    extern __shared__ __align__(16) float smem_tiles[];
+    float(*tiles)[kCH][kLd] = reinterpret_cast<float(*)[kCH][kLd]>(smem_tiles);  // [slot][row][time]
     __shared__ uint64_t done[G][kRing];
-    __shared__ float ylast_s[kTT];
+    __shared__ float ylast_s[kCH];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t r0 = (int64_t)blockIdx.x * kTT;
-    const int64_t ch = r0 + lane;
-    const bool live = ch < a.batch;
+    const int64_t r0 = (int64_t)blockIdx.x * kCH;
+    // the lane's two channels: rows lane and lane + 32 of the CTA
+    const int64_t ch[2] = {r0 + lane, r0 + kTT + lane};
+    const bool live[2] = {ch[0] < a.batch, ch[1] < a.batch};
     const int64_t n = a.n, edge = a.edge;
-    const float* __restrict__ xr = a.x + (live ? ch : 0) * a.ld_x;
 
     if (threadIdx.x == 0) {
         for (int w = 0; w < G; ++w)
@@ -180,38 +165,46 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
     }
     // sosfiltfilt: save the right-extension inputs before y (which may alias
     // x) is written, and read the first forward sample
-    float first = 0.0f;
+    float first[2] = {0.0f, 0.0f};
     if (FF) {
-        if (warp == 0 && live) {
-            const float xe = xr[n - 1];
-            for (int64_t i = 0; i < edge; ++i) a.tail[i * a.batch + ch] = 2.0f * xe - xr[n - 2 - i];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (!live[h]) continue;
+            const float* __restrict__ xr = a.x + ch[h] * a.ld_x;
+            if (warp == 0) {
+                const float xe = xr[n - 1];
+                for (int64_t i = 0; i < edge; ++i) a.tail[i * a.batch + ch[h]] = 2.0f * xe - xr[n - 2 - i];
+            }
+            first[h] = edge > 0 ? 2.0f * xr[0] - xr[edge] : xr[0];
         }
-        if (live) first = edge > 0 ? 2.0f * xr[0] - xr[edge] : xr[0];
         __threadfence_block();
     }
     __syncthreads();
 
-    float s1[SPW], s2[SPW];
-    constexpr int NP = (SPW + 1) / 2;  // coefficient pairs of this warp
-    PairSec pc[NP];
+    // states of this warp's sections for the lane's two channels (.x, .y)
+    float2 S1[SPW], S2[SPW];
+    PackSec pc[SPW];
     bool cpl[SPW];
 #pragma unroll
     for (int i = 0; i < SPW; ++i) {
         const int s = warp * SPW + i;
         // the coupled form serves complex-pole sections in FP32_COUPLED only
         cpl[i] = PREC == 3 && sc.coupled[s] != 0;
-        put_sec(pc[i / 2], i % 2, sc, s, cpl[i]);
-        if (i % 2 == 0 && i + 1 == SPW) put_sec(pc[i / 2], 1, sc, s, cpl[i]);  // unused .y half
-        s1[i] = 0.0f;
-        s2[i] = 0.0f;
-        if (!FF && a.zi && live && s < sc.nsec)
-            state_in<PREC>(sc, s, a.zi[(ch * sc.nsec + s) * 2 + 0], a.zi[(ch * sc.nsec + s) * 2 + 1],
-                           s1[i], s2[i]);
-        if (FF && a.use_zi && s < sc.nsec) {
-            const double* z = (PREC == 3 && sc.coupled[s]) ? sc.zc[s] : sc.zi[s];
-            s1[i] = (float)(z[0] * (double)first);
-            s2[i] = (float)(z[1] * (double)first);
+        put_sec(pc[i], sc, s, cpl[i]);
+        float s1v[2] = {0.0f, 0.0f}, s2v[2] = {0.0f, 0.0f};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (!FF && a.zi && live[h] && s < sc.nsec)
+                state_in<PREC>(sc, s, a.zi[(ch[h] * sc.nsec + s) * 2 + 0],
+                               a.zi[(ch[h] * sc.nsec + s) * 2 + 1], s1v[h], s2v[h]);
+            if (FF && a.use_zi && s < sc.nsec) {
+                const double* z = (PREC == 3 && sc.coupled[s]) ? sc.zc[s] : sc.zi[s];
+                s1v[h] = (float)(z[0] * (double)first[h]);
+                s2v[h] = (float)(z[1] * (double)first[h]);
+            }
         }
+        S1[i] = make_float2(s1v[0], s1v[1]);
+        S2[i] = make_float2(s2v[0], s2v[1]);
     }
 
     // this warp's section form, fixed for the launch
@@ -222,62 +215,32 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
         for (int i = 0; i < SPW; ++i) nc += cpl[i] ? 1 : 0;
         form = nc == SPW ? 1 : nc == 0 ? 0 : 2;
     }
-    // section i of the warp on one sample (i is a constant after unrolling)
-    auto step_i = [&](auto formc, int i, float v) {
+    // section i of the warp on one sample of both channels
+    auto step_i = [&](auto formc, int i, float2 v) {
         constexpr int FORM = decltype(formc)::value;
-        return (i & 1) ? sec_step<FORM, 1>(pc[i >> 1], cpl[i], s1[i], s2[i], v)
-                       : sec_step<FORM, 0>(pc[i >> 1], cpl[i], s1[i], s2[i], v);
+        if (FORM == 1 || (FORM == 2 && cpl[i])) return pack_step<true>(pc[i], S1[i], S2[i], v);
+        return pack_step<false>(pc[i], S1[i], S2[i], v);
     };
-    // Filters tn samples of this lane's channel in place through the warp's
-    // sections (a full tile fully unrolled, so the shared loads run ahead).
-    // Full tiles of an all-coupled warp with 2-4 sections go through its
-    // section pairs, one pass over the tile per pair: sample 0 of the first
-    // section alone, then 31 packed steps, then sample 31 of the second
-    // section alone.  Measured on GB300 (16,384 x 131,072, 8 sections): the
-    // coupled cascade 9.65 -> 9.12 ms; the DF2T form, whose two-operation
-    // recurrence the lockstep lengthens, 6.17 -> 9.44 ms, so it stays scalar.
-    // More sections per warp would spill registers.
-    constexpr bool kPaired = SPW >= 2 && SPW <= 4;
+    // Filters tn samples of the lane's two channels in place through the
+    // warp's sections (a full tile fully unrolled, so the shared loads run
+    // ahead and the sections of consecutive samples interleave).
     auto filter_tile = [&](auto formc, float(*t)[kLd], int tn) {
-        constexpr int FORM = decltype(formc)::value;
-        if (FORM == 1 && kPaired && tn == kTT) {
-#pragma unroll
-            for (int i = 0; i < SPW / 2; ++i) {
-                const int sa = 2 * i, sb = 2 * i + 1;
-                float2 S1 = make_float2(s1[sa], s1[sb]), S2 = make_float2(s2[sa], s2[sb]);
-                float ya = sec_step<FORM, 0>(pc[i], cpl[sa], S1.x, S2.x, t[lane][0]);
-#pragma unroll
-                for (int p = 1; p < kTT; ++p) {
-                    const float2 Y = pair_step<FORM>(pc[i], S1, S2, make_float2(t[lane][p], ya));
-                    t[lane][p - 1] = Y.y;
-                    ya = Y.x;
-                }
-                t[lane][kTT - 1] = sec_step<FORM, 1>(pc[i], cpl[sb], S1.y, S2.y, ya);
-                s1[sa] = S1.x;
-                s1[sb] = S1.y;
-                s2[sa] = S2.x;
-                s2[sb] = S2.y;
-            }
-            if (SPW % 2) {
-#pragma unroll
-                for (int p = 0; p < kTT; ++p)
-                    t[lane][p] = sec_step<FORM, 0>(pc[NP - 1], cpl[SPW - 1], s1[SPW - 1],
-                                                   s2[SPW - 1], t[lane][p]);
-            }
-        } else if (tn == kTT) {
+        if (tn == kTT) {
 #pragma unroll
             for (int p = 0; p < kTT; ++p) {
-                float v = t[lane][p];
+                float2 v = make_float2(t[lane][p], t[lane + kTT][p]);
 #pragma unroll
                 for (int i = 0; i < SPW; ++i) v = step_i(formc, i, v);
-                t[lane][p] = v;
+                t[lane][p] = v.x;
+                t[lane + kTT][p] = v.y;
             }
         } else {
             for (int p = 0; p < tn; ++p) {
-                float v = t[lane][p];
+                float2 v = make_float2(t[lane][p], t[lane + kTT][p]);
 #pragma unroll
                 for (int i = 0; i < SPW; ++i) v = step_i(formc, i, v);
-                t[lane][p] = v;
+                t[lane][p] = v.x;
+                t[lane + kTT][p] = v.y;
             }
         }
     };
@@ -292,21 +255,21 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
         constexpr int KIND = decltype(kindc)::value;
         const int64_t j0 = k * kTT, j = j0 + lane;  // this lane's stream position
         float(*t)[kLd] = tiles[slot];
-        const bool rows_full = r0 + kTT <= a.batch;
+        const bool rows_full = r0 + kCH <= a.batch;
         if (KIND == kSos && rows_full && j0 + kTT <= L) {
             const float* p = a.x + r0 * a.ld_x + j;
 #pragma unroll 8
-            for (int i = 0; i < kTT; ++i, p += a.ld_x) cp_async4(&t[i][lane], p, true);
+            for (int i = 0; i < kCH; ++i, p += a.ld_x) cp_async4(&t[i][lane], p, true);
         } else if (KIND == kFwd && rows_full && j0 >= edge && j0 + kTT <= edge + n) {
             const float* p = a.x + r0 * a.ld_x + (j - edge);
 #pragma unroll 8
-            for (int i = 0; i < kTT; ++i, p += a.ld_x) cp_async4(&t[i][lane], p, true);
+            for (int i = 0; i < kCH; ++i, p += a.ld_x) cp_async4(&t[i][lane], p, true);
         } else if (KIND == kBwd && rows_full && j0 >= edge && j0 + kTT <= L) {
             const float* p = a.y + r0 * a.ld_y + (n - 1 - (j - edge));
 #pragma unroll 8
-            for (int i = 0; i < kTT; ++i, p += a.ld_y) cp_async4(&t[i][lane], p, true);
+            for (int i = 0; i < kCH; ++i, p += a.ld_y) cp_async4(&t[i][lane], p, true);
         } else {
-            for (int i = 0; i < kTT; ++i) {
+            for (int i = 0; i < kCH; ++i) {
                 const int64_t row = r0 + i;
                 const bool vr = row < a.batch && j < L;
                 const float* rx = a.x + (row < a.batch ? row : 0) * a.ld_x;
@@ -339,7 +302,7 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
         constexpr int KIND = decltype(kindc)::value;
         const int64_t j0 = k * kTT, j = j0 + lane;
         float(*t)[kLd] = tiles[slot];
-        const bool rows_full = r0 + kTT <= a.batch;
+        const bool rows_full = r0 + kCH <= a.batch;
         float* q = nullptr;
         if (KIND == kSos && rows_full && j0 + kTT <= L) q = a.y + r0 * a.ld_y + j;
         if (KIND == kFwd && rows_full && j0 >= edge && j0 + kTT <= edge + n)
@@ -348,13 +311,13 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
             q = a.y + r0 * a.ld_y + (n - 1 - (j - edge));
         if (q) {
 #pragma unroll 8
-            for (int i = 0; i < kTT; ++i, q += a.ld_y) *q = t[i][lane];
+            for (int i = 0; i < kCH; ++i, q += a.ld_y) *q = t[i][lane];
             // the forward stream's last output seeds the backward pass (edge == 0)
             if (KIND == kFwd && j == L - 1)
-                for (int i = 0; i < kTT; ++i) ylast_s[i] = t[i][lane];
+                for (int i = 0; i < kCH; ++i) ylast_s[i] = t[i][lane];
             return;
         }
-        for (int i = 0; i < kTT; ++i) {
+        for (int i = 0; i < kCH; ++i) {
             const int64_t row = r0 + i;
             if (row >= a.batch || j >= L) continue;
             const float v = t[i][lane];
@@ -426,15 +389,19 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
 
     if (!FF) {
         run(std::integral_constant<int, kSos>(), n);
-        if (a.zf && live) {
+        if (a.zf) {
 #pragma unroll
             for (int i = 0; i < SPW; ++i) {
                 const int s = warp * SPW + i;
-                if (s < sc.nsec) {
+                if (s >= sc.nsec) continue;
+                const float u1[2] = {S1[i].x, S1[i].y}, u2[2] = {S2[i].x, S2[i].y};
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (!live[h]) continue;
                     double o1, o2;
-                    state_out<PREC>(sc, s, s1[i], s2[i], o1, o2);
-                    a.zf[(ch * sc.nsec + s) * 2 + 0] = o1;
-                    a.zf[(ch * sc.nsec + s) * 2 + 1] = o2;
+                    state_out<PREC>(sc, s, u1[h], u2[h], o1, o2);
+                    a.zf[(ch[h] * sc.nsec + s) * 2 + 0] = o1;
+                    a.zf[(ch[h] * sc.nsec + s) * 2 + 1] = o2;
                 }
             }
         }
@@ -442,14 +409,16 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
     }
     run(std::integral_constant<int, kFwd>(), n + 2 * edge);
     // backward initial state from the last forward output
-    const float yl = ylast_s[lane];
+    const float yl[2] = {ylast_s[lane], ylast_s[lane + kTT]};
 #pragma unroll
     for (int i = 0; i < SPW; ++i) {
         const int s = warp * SPW + i;
         const bool on = a.use_zi && s < sc.nsec;
         const double* z = (PREC == 3 && sc.coupled[s]) ? sc.zc[s] : sc.zi[s];
-        s1[i] = on ? (float)(z[0] * (double)yl) : 0.0f;
-        s2[i] = on ? (float)(z[1] * (double)yl) : 0.0f;
+        S1[i] = on ? make_float2((float)(z[0] * (double)yl[0]), (float)(z[0] * (double)yl[1]))
+                   : make_float2(0.0f, 0.0f);
+        S2[i] = on ? make_float2((float)(z[1] * (double)yl[0]), (float)(z[1] * (double)yl[1]))
+                   : make_float2(0.0f, 0.0f);
     }
     run(std::integral_constant<int, kBwd>(), n + edge);
 }
@@ -460,14 +429,16 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
 
 template <int NS, int PREC, bool FF>
 int run_pipe(const SosCoef& c, const PipeArgs& a, cudaStream_t st) {
-    const int64_t grid = ceil_div(a.batch, kTT);
-    // The CTAs are few (one per 32 channels) and each holds a 34 KB ring:
-    // with the default carveout only two fit an SM (measured: 16,384 channels
-    // ran in two waves), so ask for the largest shared-memory carveout.
-    SCIR_CUDA_TRY(cudaFuncSetAttribute(sos_pipe_kernel<NS, PREC, FF>,
-                                       cudaFuncAttributePreferredSharedMemoryCarveout,
+    const int64_t grid = ceil_div(a.batch, kCH);
+    // One CTA per 64 channels, each with a (G + 4)-slot ring of 64 x 33
+    // floats (68 KB for 4 warps): ask for the largest shared-memory carveout
+    // so two CTAs fit an SM.
+    const size_t smem = sizeof(float) * (size_t)PipeShape<NS>::kRing * kCH * kLd;
+    auto kern = sos_pipe_kernel<NS, PREC, FF>;
+    SCIR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    SCIR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                        (int)cudaSharedmemCarveoutMaxShared));
-    sos_pipe_kernel<NS, PREC, FF><<<(unsigned)grid, 32 * PipeShape<NS>::G, 0, st>>>(c, a);
+    kern<<<(unsigned)grid, 32 * PipeShape<NS>::G, smem, st>>>(c, a);
     SCIR_LAUNCH_CHECK("sos_pipe_kernel");
     return SCIR_OK;
 }

@@ -195,3 +195,30 @@ def test_fp32_cascade_lengths(cuda, n, order):
             assert normwise_err(ynp, ref_np) < tol_ff, (prec, "unpadded")
         else:
             assert np.all(np.abs(ynp) < 1e-30), (prec, "unpadded, underflow")
+
+
+# Two channels per lane (rows l and l + 32 of a 64-channel CTA): batches
+# that fill both halves, leave the second half partly empty, and span many
+# CTAs -- including a full-size-width case of 4,160 channels (65 CTAs).
+@pytest.mark.parametrize("batch", [33, 64, 100, 4160])
+def test_fp32_pipe_channel_halves(cuda, batch):
+    import torch
+    rng = np.random.default_rng(batch)
+    n = 3000 if batch > 1000 else 7000
+    x = rng.standard_normal((batch, n)).astype(np.float32)
+    rows = sorted({0, 31, 32, 33, 63, batch // 2, batch - 33, batch - 32, batch - 1} &
+                  set(range(batch)))
+    x64 = x[rows].astype(np.float64)
+    P = S.SosPrecision.FP32_COUPLED
+    y = S.sosfilt_f32(SOS5, _dev(x, cuda), precision=P).cpu().numpy()
+    assert normwise_err(y[rows], O.sosfilt_f64(SOS5, x64)) < TOL
+    # every row against the row-by-row FP32 result of single-channel calls
+    for r in rows[:4]:
+        yr = S.sosfilt_f32(SOS5, _dev(x[r:r + 1], cuda), precision=P).cpu().numpy()
+        assert np.array_equal(yr[0], y[r])
+    xd = _dev(x, cuda)
+    S.sosfiltfilt_f32(SOS5, xd, precision=P, out=xd)  # in place
+    assert normwise_err(xd.cpu().numpy()[rows], O.sosfiltfilt_f64(SOS5, x64)) < TOL
+    ydf = S.sosfilt_f32(SOS5, _dev(x, cuda), precision=S.SosPrecision.FP32).cpu().numpy()
+    assert np.all(np.isfinite(ydf))
+    del torch
