@@ -3,14 +3,15 @@
 //
 // Contraction.  Outputs are grouped in windows of 1,024 (o0 .. o0+1023) and
 // split by output phase phi = r mod 8 (r = o - o0 = 8u + phi, u < 128).  For
-// one phase, with u' = 127 - u and the signal window starting at the 16-byte
-// aligned sample xa = o0 + s - m (m = s mod 4, the same for every window):
+// one phase, with u' = 127 - u and the signal window starting at the sample
+// xa = o0 + s - m (m = s mod 8, the same for every window, so xa is a
+// multiple of 8 -- 16 bytes of bf16 -- as a TMA coordinate must be):
 //   y[b][o0 + r] = sum_J X[b][xa + J] * c[J - m - r]
 //                = sum_J A[b][J] * B_phi[u'][J],   B_phi[u'][J] = G_phi[8u' + J],
 //   G_phi[i] = c[i - 8*127 - phi - m]  (zero outside [0, k)).
-// A (128 channels x 64 samples per K chunk, K-major, 128-byte swizzle) is
-// written into shared memory by converter warps straight from the f32 rows
-// in global memory, split into bf16 terms on the way.  B_phi is a Hankel
+// A (128 channels x 64 samples per K chunk, K-major, 128-byte swizzle) is a
+// TMA box of the signal's bf16 term planes, which a split kernel writes once
+// per call (x = x1 + x2 [+ x3]).  B_phi is a Hankel
 // matrix whose rows shift by 8 bf16 = 16 bytes: exactly the no-swizzle K-major
 // core-matrix layout with a 16-byte leading (K) offset and a 128-byte stride
 // (N) offset, so B_phi is a descriptor into a contiguous tap window in shared
@@ -35,15 +36,21 @@
 // groups of a window are consecutive tile indices, so they run on
 // neighbouring SMs at the same time and share the signal rows in L2.
 //
-// Roles (448 threads, one CTA per SM, persistent over tiles):
-//   warp 0     bulk-copies the tile's tap windows (two phases x terms) per K
-//              chunk into an N-stage ring (B full barrier with tx count);
+// Why planes in memory rather than a split inside this kernel: the MMAs
+// read their A and B tiles from shared memory at about the rate shared
+// memory delivers, so every other shared-memory access slows them.  A
+// variant whose converter warps loaded the f32 rows and stored the bf16
+// terms into the A layout themselves was measured at 11.0 ms (BF16X6) /
+// 7.3 ms (BF16X3) on 1,024 x 262,144 x 4,095 against 9.5 / 6.0 ms for TMA
+// loads of pre-split planes: the loads through L1 and the stores competed
+// with the operand reads.
+//
+// Roles (320 threads, one CTA per SM, persistent over tiles):
+//   warp 0     TMA producer: per K chunk the signal box of every term and the
+//              tile's tap windows (two phases x terms) into an N-stage ring
+//              (full barrier with tx count);
 //   warp 1     one thread issues the MMAs and commits stages and tiles;
-//   warps 2-5  converters: each K chunk's 128 x 64 f32 signal block, loaded
-//              with 16-byte global loads one chunk ahead, split into bf16
-//              terms and stored in the 128-byte-swizzled A layout (A full
-//              barrier, one arrival per warp);
-//   warps 6-13 epilogue: tcgen05.ld of both accumulators (two warps per TMEM
+//   warps 2-9  epilogue: tcgen05.ld of both accumulators (two warps per TMEM
 //              lane quarter, each half of the columns), the sum, one 8-byte
 //              store of the tile's two adjacent phases per column, TMEM zeroed.
 // Every wait is bounded; a timeout sets the device error word and the CTA
@@ -69,20 +76,67 @@ constexpr int kGroups = kPh / kPhT;  // phase groups per window
 constexpr int kNCOL = kPh * kU;  // outputs per window
 constexpr int kWB = kKC + 8 * kU;  // tap window per phase per chunk (elements)
 constexpr uint32_t kBBytesPh = kWB * 2;
-constexpr int kConvWarps = 4;
 constexpr int kEpiWarps = 8;
-constexpr int kThreads = 32 * (2 + kConvWarps + kEpiWarps);
+constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr int kTmemCols = 512;
 constexpr uint32_t kABytesTerm = kM * kKC * 2;  // 16 KB
 constexpr int kCrossCol = kPhT * kU;            // first column of the cross accumulators
 
 struct TcGeom {
     int nstage, nchunks, m;
-    int64_t xa0, n, n_out, batch, ld_x, LG, k;
+    int64_t xa0, n_out, batch, LG, k;
     int64_t blocks_per_cg, n_tiles;  // windows per channel group; tiles in total
-    uint32_t stage_bytes, b_bytes;
-    int vec_load, vec_store;
+    uint32_t stage_bytes, tx_bytes;
+    int vec_store;
 };
+
+// Splits 4 floats into 2 or 3 bf16 terms, each packed as 4 bf16 (8 bytes).
+__device__ __forceinline__ void split4_any(const float4 v, int terms, uint2 (&out)[3]) {
+    const __nv_bfloat162 a1 = __floats2bfloat162_rn(v.x, v.y);
+    const __nv_bfloat162 b1 = __floats2bfloat162_rn(v.z, v.w);
+    const float2 fa1 = __bfloat1622float2(a1), fb1 = __bfloat1622float2(b1);
+    const float ra0 = v.x - fa1.x, ra1 = v.y - fa1.y, rb0 = v.z - fb1.x, rb1 = v.w - fb1.y;
+    const __nv_bfloat162 a2 = __floats2bfloat162_rn(ra0, ra1);
+    const __nv_bfloat162 b2 = __floats2bfloat162_rn(rb0, rb1);
+    out[0].x = *reinterpret_cast<const uint32_t*>(&a1);
+    out[0].y = *reinterpret_cast<const uint32_t*>(&b1);
+    out[1].x = *reinterpret_cast<const uint32_t*>(&a2);
+    out[1].y = *reinterpret_cast<const uint32_t*>(&b2);
+    out[2] = make_uint2(0u, 0u);
+    if (terms == 3) {
+        const float2 fa2 = __bfloat1622float2(a2), fb2 = __bfloat1622float2(b2);
+        const __nv_bfloat162 a3 = __floats2bfloat162_rn(ra0 - fa2.x, ra1 - fa2.y);
+        const __nv_bfloat162 b3 = __floats2bfloat162_rn(rb0 - fb2.x, rb1 - fb2.y);
+        out[2].x = *reinterpret_cast<const uint32_t*>(&a3);
+        out[2].y = *reinterpret_cast<const uint32_t*>(&b3);
+    }
+}
+
+// x -> bf16 term planes xs[t][b][i] = term t of x[b][i] (zero for
+// n <= i < nA).  Each thread converts 4 consecutive elements: the loads are
+// coalesced across the warp and each plane gets one 8-byte store.
+__global__ void split_signal_kernel(const float* __restrict__ x, int64_t ld_x, int64_t batch,
+                                    int64_t n, int64_t nA, int terms,
+                                    __nv_bfloat16* __restrict__ xs) {
+    const int64_t plane = batch * nA;
+    const int64_t groups = nA / 4;  // nA is a multiple of 8
+    for (int64_t b = blockIdx.y; b < batch; b += gridDim.y) {
+        const float* __restrict__ xr = x + b * ld_x;
+        for (int64_t gi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gi < groups;
+             gi += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t i0 = gi * 4;
+            float e[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) e[j] = i0 + j < n ? __ldg(xr + i0 + j) : 0.0f;
+            uint2 t3[3];
+            split4_any(make_float4(e[0], e[1], e[2], e[3]), terms, t3);
+            const int64_t o = b * nA + i0;
+#pragma unroll
+            for (int t = 0; t < 3; ++t)
+                if (t < terms) *reinterpret_cast<uint2*>(xs + t * plane + o) = t3[t];
+        }
+    }
+}
 
 // Tap operand planes G[t][phi][i] = term t of c[i - 8*(U-1) - phi - m]
 // (zero outside [0, k)), c = taps or reversed taps.
@@ -113,28 +167,6 @@ __host__ __device__ constexpr int prod_b(int p) {
     return p == 0 ? 0 : p == 1 ? 1 : p == 2 ? 0 : p == 3 ? 2 : p == 4 ? 1 : 0;
 }
 
-// Splits 4 floats into T bf16 terms, each packed as 4 bf16 (8 bytes).
-template <int T>
-__device__ __forceinline__ void split4(const float4 v, uint2 (&out)[3]) {
-    const __nv_bfloat162 a1 = __floats2bfloat162_rn(v.x, v.y);
-    const __nv_bfloat162 b1 = __floats2bfloat162_rn(v.z, v.w);
-    const float2 fa1 = __bfloat1622float2(a1), fb1 = __bfloat1622float2(b1);
-    const float ra0 = v.x - fa1.x, ra1 = v.y - fa1.y, rb0 = v.z - fb1.x, rb1 = v.w - fb1.y;
-    const __nv_bfloat162 a2 = __floats2bfloat162_rn(ra0, ra1);
-    const __nv_bfloat162 b2 = __floats2bfloat162_rn(rb0, rb1);
-    out[0].x = *reinterpret_cast<const uint32_t*>(&a1);
-    out[0].y = *reinterpret_cast<const uint32_t*>(&b1);
-    out[1].x = *reinterpret_cast<const uint32_t*>(&a2);
-    out[1].y = *reinterpret_cast<const uint32_t*>(&b2);
-    if (T == 3) {
-        const float2 fa2 = __bfloat1622float2(a2), fb2 = __bfloat1622float2(b2);
-        const __nv_bfloat162 a3 = __floats2bfloat162_rn(ra0 - fa2.x, ra1 - fa2.y);
-        const __nv_bfloat162 b3 = __floats2bfloat162_rn(rb0 - fb2.x, rb1 - fb2.y);
-        out[2].x = *reinterpret_cast<const uint32_t*>(&a3);
-        out[2].y = *reinterpret_cast<const uint32_t*>(&b3);
-    }
-}
-
 // Live 16-row groups [lo, hi) (multiples of 16) of phase operand phi for
 // the K step starting at J0: rows u' whose 16 taps G_phi[8u' + J0 ..] meet
 // the non-zero range [L0, L0 + k) of G_phi.
@@ -151,15 +183,14 @@ __device__ __forceinline__ void live_rows(int64_t J0, int64_t L0, int64_t k, int
 
 template <int T>  // bf16 terms per operand: 2 (BF16X3) or 3 (BF16X6)
 __global__ void __launch_bounds__(kThreads, 1)
-fir_tc_kernel(const float* __restrict__ x, const __nv_bfloat16* __restrict__ G, const TcGeom g,
-              float* __restrict__ y, int64_t ld_y, unsigned* __restrict__ err) {
+fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __restrict__ G,
+              const TcGeom g, float* __restrict__ y, int64_t ld_y, unsigned* __restrict__ err) {
     constexpr int NPROD = T == 2 ? 3 : 6;
     constexpr uint32_t kABytes = T * kABytesTerm;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
-    uint64_t* fullA = reinterpret_cast<uint64_t*>(base + (size_t)g.nstage * g.stage_bytes);
-    uint64_t* fullB = fullA + g.nstage;
-    uint64_t* empty = fullB + g.nstage;
+    uint64_t* full = reinterpret_cast<uint64_t*>(base + (size_t)g.nstage * g.stage_bytes);
+    uint64_t* empty = full + g.nstage;
     uint64_t* tfull = empty + g.nstage;
     uint64_t* tempty = tfull + 1;
     uint64_t* mma_done = tempty + 1;
@@ -169,8 +200,7 @@ fir_tc_kernel(const float* __restrict__ x, const __nv_bfloat16* __restrict__ G, 
     if (warp == 0) {
         if (lane == 0) {
             for (int s = 0; s < g.nstage; ++s) {
-                mbar_init(&fullA[s], kConvWarps);
-                mbar_init(&fullB[s], 1);
+                mbar_init(&full[s], 1);
                 mbar_init(&empty[s], 1);
             }
             mbar_init(tfull, 1);
@@ -188,12 +218,16 @@ fir_tc_kernel(const float* __restrict__ x, const __nv_bfloat16* __restrict__ G, 
     const uint32_t tmem = *tmem_slot;
 
     if (warp == 0) {
-        // ------------------------------------------------ tap windows (bulk copies)
+        // ------------------------------------------------ TMA producer
         if (lane == 0) {
+            prefetch_tmap(&amap);
             uint32_t it = 0;
             bool ok = true;
             for (int64_t tile = blockIdx.x; ok && tile < g.n_tiles; tile += gridDim.x) {
                 const int pg = (int)(tile % kGroups);
+                const int64_t w = tile / kGroups;
+                const int64_t cg = w / g.blocks_per_cg, blk = w % g.blocks_per_cg;
+                const int64_t xc0 = g.xa0 + blk * kNCOL;
                 for (int c = 0; c < g.nchunks; ++c, ++it) {
                     const int st = (int)(it % (uint32_t)g.nstage);
                     const uint32_t ph = (it / (uint32_t)g.nstage) & 1u;
@@ -202,8 +236,13 @@ fir_tc_kernel(const float* __restrict__ x, const __nv_bfloat16* __restrict__ G, 
                         ok = false;
                         break;
                     }
-                    uint8_t* bb = base + (size_t)st * g.stage_bytes + kABytes;
-                    mbar_arrive_expect_tx(&fullB[st], g.b_bytes);
+                    uint8_t* sb = base + (size_t)st * g.stage_bytes;
+                    mbar_arrive_expect_tx(&full[st], g.tx_bytes);
+#pragma unroll
+                    for (int t = 0; t < T; ++t)
+                        tma_load_3d(sb + t * kABytesTerm, &amap, &full[st],
+                                    (int32_t)(xc0 + (int64_t)c * kKC), (int32_t)(cg * kM), t);
+                    uint8_t* bb = sb + kABytes;
 #pragma unroll
                     for (int t = 0; t < T; ++t)
 #pragma unroll
@@ -211,13 +250,13 @@ fir_tc_kernel(const float* __restrict__ x, const __nv_bfloat16* __restrict__ G, 
                             bulk_load(bb + (t * kPhT + l) * kBBytesPh,
                                       G + ((int64_t)(t * kPh + kPhT * pg + l) * g.LG +
                                            (int64_t)c * kKC),
-                                      kBBytesPh, &fullB[st]);
+                                      kBBytesPh, &full[st]);
                 }
             }
             // the copies issued last have landed before this thread leaves
             const uint32_t first = it > (uint32_t)g.nstage ? it - (uint32_t)g.nstage : 0u;
             for (uint32_t j = first; j < it; ++j)
-                if (!mbar_wait(&fullB[j % (uint32_t)g.nstage], (j / (uint32_t)g.nstage) & 1u))
+                if (!mbar_wait(&full[j % (uint32_t)g.nstage], (j / (uint32_t)g.nstage) & 1u))
                     atomicOr(err, kErrMbarTimeout);
         }
     } else if (warp == 1) {
@@ -237,7 +276,7 @@ fir_tc_kernel(const float* __restrict__ x, const __nv_bfloat16* __restrict__ G, 
                 for (int c = 0; c < g.nchunks; ++c, ++it) {
                     const int st = (int)(it % (uint32_t)g.nstage);
                     const uint32_t ph = (it / (uint32_t)g.nstage) & 1u;
-                    if (!mbar_wait(&fullB[st], ph) || !mbar_wait(&fullA[st], ph)) {
+                    if (!mbar_wait(&full[st], ph)) {
                         atomicOr(err, kErrMbarTimeout);
                         ok = false;
                         break;
@@ -276,73 +315,10 @@ fir_tc_kernel(const float* __restrict__ x, const __nv_bfloat16* __restrict__ G, 
             tc_commit(mma_done);
             if (!mbar_wait(mma_done, 0)) atomicOr(err, kErrMbarTimeout);
         }
-    } else if (warp < 2 + kConvWarps) {
-        // ------------------------------------------------ converters
-        const int cw = warp - 2;
-        const int rr = lane >> 4, q4 = lane & 15;  // row parity, float4 index in the chunk row
-        float4 v[16];
-        uint32_t it = 0;
-        bool ok = true;
-        // 16 rows of this thread in chunk c of tile `tile`: rows 32cw + 2i + rr,
-        // samples xa + 64c + 4q4 .. +4 (zero outside the signal)
-        auto load = [&](int64_t tile, int c) {
-            const int64_t w = tile / kGroups;
-            const int64_t cg = w / g.blocks_per_cg, blk = w % g.blocks_per_cg;
-            const int64_t p = g.xa0 + blk * kNCOL + (int64_t)c * kKC + 4 * q4;
-            const bool inside = p >= 0 && p + 4 <= g.n;
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                const int64_t row = cg * kM + 32 * cw + 2 * i + rr;
-                const float* xr = x + row * g.ld_x;
-                if (row < g.batch && inside && g.vec_load) {
-                    v[i] = __ldg(reinterpret_cast<const float4*>(xr + p));
-                } else {
-                    float e[4];
-#pragma unroll
-                    for (int j = 0; j < 4; ++j)
-                        e[j] = (row < g.batch && p + j >= 0 && p + j < g.n) ? __ldg(xr + p + j) : 0.0f;
-                    v[i] = make_float4(e[0], e[1], e[2], e[3]);
-                }
-            }
-        };
-        int64_t tile = blockIdx.x;
-        int c = 0;
-        if (tile < g.n_tiles) load(tile, 0);
-        while (ok && tile < g.n_tiles) {
-            const int st = (int)(it % (uint32_t)g.nstage);
-            const uint32_t ph = (it / (uint32_t)g.nstage) & 1u;
-            if (!__all_sync(0xffffffffu, mbar_wait(&empty[st], ph ^ 1u))) {
-                if (lane == 0) atomicOr(err, kErrMbarTimeout);
-                ok = false;
-                break;
-            }
-            uint8_t* sa = base + (size_t)st * g.stage_bytes;
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                const int r = 32 * cw + 2 * i + rr;
-                uint2 t3[3];
-                split4<T>(v[i], t3);
-                // 128-byte swizzle: 16-byte unit index XOR (row mod 8)
-                const uint32_t off = (uint32_t)r * 128u + ((uint32_t)((q4 >> 1) ^ (r & 7)) << 4) +
-                                     (uint32_t)(q4 & 1) * 8u;
-#pragma unroll
-                for (int t = 0; t < T; ++t)
-                    *reinterpret_cast<uint2*>(sa + t * kABytesTerm + off) = t3[t];
-            }
-            fence_proxy_async_smem();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&fullA[st]);
-            ++it;
-            if (++c == g.nchunks) {
-                c = 0;
-                tile += gridDim.x;
-            }
-            if (tile < g.n_tiles) load(tile, c);  // one chunk ahead
-        }
     } else {
         // ------------------------------------------------ epilogue
-        const int q = warp & 3;                              // TMEM lane quarter
-        const int half = (warp - 2 - kConvWarps) >> 2;       // which 64 of a phase's 128 columns
+        const int q = warp & 3;                   // TMEM lane quarter
+        const int half = (warp - 2) >> 2;         // which 64 of a phase's 128 columns
         const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16);
         // the accumulators start at zero (every MMA accumulates)
 #pragma unroll 1
@@ -417,45 +393,61 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
     int rc = current_device(&info);
     if (rc) return rc;
     TcGeom g;
-    g.m = (int)(((a.s % 4) + 4) % 4);
+    g.m = (int)(((a.s % 8) + 8) % 8);
     g.xa0 = a.s - g.m;
-    g.n = a.n;
     g.k = a.k;
-    g.ld_x = a.ld_x;
     g.n_out = a.n_out;
     g.batch = a.batch;
+    const int64_t nA = (a.n + 7) / 8 * 8;
     const int64_t ktot = a.k + kNCOL - 1 + g.m;
     g.nchunks = (int)ceil_div(ktot, kKC);
     g.LG = (int64_t)g.nchunks * kKC + 8 * kU;
     g.blocks_per_cg = ceil_div(a.n_out, kNCOL);
     g.n_tiles = g.blocks_per_cg * ceil_div(a.batch, kM) * kGroups;
-    g.vec_load = ((reinterpret_cast<uintptr_t>(a.x) & 15) == 0 && (a.ld_x % 4) == 0) ? 1 : 0;
     g.vec_store = ((reinterpret_cast<uintptr_t>(a.y) & 7) == 0 && (a.ld_y % 2) == 0) ? 1 : 0;
-    if (g.nchunks >= (1 << 30) || g.n_tiles >= (1LL << 40))
-        return set_error(SCIR_ERR_UNSUPPORTED, "tensor-core FIR geometry too large");
+    // TMA coordinates are 32-bit: the last window's K range and the channel
+    // groups must stay below 2^31
+    if (nA + 2 * kNCOL + ktot >= (1LL << 31) || ceil_div(a.batch, kM) * kM >= (1LL << 31))
+        return set_error(SCIR_ERR_UNSUPPORTED, "tensor-core FIR coordinates exceed 32 bits");
     unsigned* err = device_error_word();
     if (!err) return set_error(SCIR_ERR_CUDA, "device error word unavailable");
 
-    const uint32_t b_bytes = T * kPhT * kBBytesPh;
-    const uint32_t stage = T * kABytesTerm + b_bytes;
+    const uint32_t stage = T * kABytesTerm + T * kPhT * kBBytesPh;
     g.stage_bytes = (stage + 1023) / 1024 * 1024;
-    g.b_bytes = b_bytes;
-    const size_t extra = 1024 + 8 * (3 * 8 + 3) + 16;
+    g.tx_bytes = stage;
+    const size_t extra = 1024 + 8 * (2 * 8 + 3) + 16;
     const int nstage =
         (int)std::min<int64_t>(8, (info->max_smem_optin - (int64_t)extra) / g.stage_bytes);
     if (nstage < 2) return set_error(SCIR_ERR_UNSUPPORTED, "tensor-core FIR stage too large");
     g.nstage = nstage;
     const size_t smem = (size_t)nstage * g.stage_bytes + extra;
 
-    // the tap operand planes (a few hundred KB) into scratch memory
+    // the signal's term planes and the tap operand planes into scratch memory
+    __nv_bfloat16* xs = nullptr;
     __nv_bfloat16* Gs = nullptr;
+    const size_t xs_bytes = sizeof(__nv_bfloat16) * (size_t)T * (size_t)a.batch * (size_t)nA;
     const size_t g_bytes = sizeof(__nv_bfloat16) * (size_t)T * kPh * (size_t)g.LG;
-    rc = scratch_alloc((void**)&Gs, g_bytes, st);
+    rc = scratch_alloc((void**)&xs, xs_bytes, st);
     if (rc) return rc;
-    const unsigned gt = (unsigned)std::min<int64_t>(ceil_div((int64_t)kPh * g.LG, 256), 4096);
-    split_taps_kernel<<<gt, 256, 0, st>>>(a.taps, a.k, a.reverse, g.m, g.LG, T, Gs);
-    cudaError_t le = cudaGetLastError();
-    if (le != cudaSuccess) rc = set_error(SCIR_ERR_CUDA, "split_taps_kernel: %s", cudaGetErrorString(le));
+    rc = scratch_alloc((void**)&Gs, g_bytes, st);
+    if (rc) {
+        scratch_free(xs, st);
+        return rc;
+    }
+    CUtensorMap amap;
+    rc = make_tmap_3d(&amap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, xs, (uint64_t)nA, (uint64_t)a.batch,
+                      (uint64_t)T, (uint64_t)nA * 2, (uint64_t)nA * 2 * (uint64_t)a.batch, kKC, kM,
+                      1, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (rc == SCIR_OK) {
+        const unsigned gx = (unsigned)std::min<int64_t>(ceil_div(nA / 4, 256), 4096);
+        const unsigned gy = (unsigned)std::min<int64_t>(a.batch, 65535);
+        split_signal_kernel<<<dim3(gx, gy), 256, 0, st>>>(a.x, a.ld_x, a.batch, a.n, nA, T, xs);
+        const unsigned gt = (unsigned)std::min<int64_t>(ceil_div((int64_t)kPh * g.LG, 256), 4096);
+        split_taps_kernel<<<gt, 256, 0, st>>>(a.taps, a.k, a.reverse, g.m, g.LG, T, Gs);
+        cudaError_t le = cudaGetLastError();
+        if (le != cudaSuccess)
+            rc = set_error(SCIR_ERR_CUDA, "split kernels: %s", cudaGetErrorString(le));
+    }
     if (rc == SCIR_OK) {
         auto kern = fir_tc_kernel<T>;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -466,13 +458,14 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
                            cudaGetErrorString(e));
         } else {
             const int64_t grid = std::min<int64_t>(g.n_tiles, (int64_t)info->sm_count);
-            kern<<<(unsigned)grid, kThreads, smem, st>>>(a.x, Gs, g, a.y, a.ld_y, err);
-            le = cudaGetLastError();
+            kern<<<(unsigned)grid, kThreads, smem, st>>>(amap, Gs, g, a.y, a.ld_y, err);
+            cudaError_t le = cudaGetLastError();
             if (le != cudaSuccess)
                 rc = set_error(SCIR_ERR_CUDA, "launch of fir_tc_kernel failed: %s",
                                cudaGetErrorString(le));
         }
     }
+    scratch_free(xs, st);
     scratch_free(Gs, st);
     return rc;
 }
@@ -480,7 +473,7 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
 }  // namespace
 
 bool fir_tc_supported(const FirArgs& a) {
-    return a.k >= 1 && a.n >= 1 && a.batch >= 1 && a.n_out >= 1 && a.n < (1LL << 40);
+    return a.k >= 1 && a.n >= 1 && a.batch >= 1 && a.n_out >= 1 && a.n < (1LL << 30);
 }
 
 int launch_fir_tc(const FirArgs& a, int terms, cudaStream_t st) {

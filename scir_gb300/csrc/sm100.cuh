@@ -136,6 +136,10 @@ __device__ __forceinline__ void bulk_commit() {
 __device__ __forceinline__ void bulk_wait_read1() {
     asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
 }
+// Waits until no bulk group of this thread still reads shared memory.
+__device__ __forceinline__ void bulk_wait_read0() {
+    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
 // Waits until every bulk group of this thread has completed.
 __device__ __forceinline__ void bulk_wait_all() {
     asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");

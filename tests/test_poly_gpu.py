@@ -198,3 +198,24 @@ def test_resample_tc_cfg2_full_size(cuda):
     err = normwise_err(y[rows].cpu().numpy(), ref)
     print(f"tensor-core resample cfg2: normwise error {err:.2e}")
     assert err < TOL_TC
+
+
+# ------------------------------------- compile-time 160/147 kernel (default design)
+# resample_poly(x, 160, 147) with the default 3,201-tap design runs a kernel
+# whose rates, phases and tap counts are compile-time constants (items of one
+# channel x 32 periods).  Lengths below cover a partial first item, item and
+# period boundaries (4,704 inputs per item), rows shorter than the filter and
+# a length that is not a multiple of 4.
+@pytest.mark.parametrize("n", [1, 2, 37, 1600, 4703, 4704, 4705, 9409, 150001])
+@pytest.mark.parametrize("batch", [1, 3])
+def test_resample_fixed_rate_lengths(cuda, n, batch):
+    rng = np.random.default_rng(n + batch)
+    x = rng.standard_normal((batch, n)).astype(np.float32)
+    h = S.resample_poly_default_taps(160, 147).astype(np.float32)
+    ref = O.resample_poly_fast_f64(x.astype(np.float64), 160, 147, h.astype(np.float64))
+    y = S.resample_poly_f32(_dev(x, cuda), 160, 147).cpu().numpy()
+    assert y.shape == ref.shape
+    assert normwise_err(y, ref) < TOL_FP32
+    # the same taps passed explicitly run the streaming kernel: the two agree
+    y2 = S.resample_poly_f32(_dev(x, cuda), 160, 147, h=_dev(h, cuda)).cpu().numpy()
+    assert normwise_err(y, y2) < 1e-6
