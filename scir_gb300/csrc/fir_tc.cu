@@ -45,14 +45,15 @@
 // loads of pre-split planes: the loads through L1 and the stores competed
 // with the operand reads.
 //
-// Roles (320 threads, one CTA per SM, persistent over tiles):
+// Roles (576 threads, one CTA per SM, persistent over tiles):
 //   warp 0     TMA producer: per K chunk the signal box of every term and the
 //              tile's tap windows (two phases x terms) into an N-stage ring
 //              (full barrier with tx count);
 //   warp 1     one thread issues the MMAs and commits stages and tiles;
-//   warps 2-9  epilogue: tcgen05.ld of both accumulators (two warps per TMEM
-//              lane quarter, each half of the columns), the sum, one 8-byte
-//              store of the tile's two adjacent phases per column, TMEM zeroed.
+//   warps 2-17 epilogue: tcgen05.ld of both accumulators (four warps per
+//              TMEM lane quarter, 32 columns each), the sum into registers,
+//              TMEM zeroed and released to the MMA thread, then one 8-byte
+//              store of the tile's two adjacent phases per column.
 // Every wait is bounded; a timeout sets the device error word and the CTA
 // leaves its loops; the producer first waits (bounded) for its copies in
 // flight and the MMA thread for its MMAs, then TMEM is freed.
@@ -76,7 +77,7 @@ constexpr int kGroups = kPh / kPhT;  // phase groups per window
 constexpr int kNCOL = kPh * kU;  // outputs per window
 constexpr int kWB = kKC + 8 * kU;  // tap window per phase per chunk (elements)
 constexpr uint32_t kBBytesPh = kWB * 2;
-constexpr int kEpiWarps = 8;
+constexpr int kEpiWarps = 16;      // four per TMEM lane quarter
 constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr int kTmemCols = 512;
 constexpr uint32_t kABytesTerm = kM * kKC * 2;  // 16 KB
@@ -317,16 +318,20 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
         }
     } else {
         // ------------------------------------------------ epilogue
-        const int q = warp & 3;                   // TMEM lane quarter
-        const int half = (warp - 2) >> 2;         // which 64 of a phase's 128 columns
+        constexpr int kCols = kU / (kEpiWarps / 4);   // columns of a phase per warp
+        constexpr int kGrp = kCols / 16;
+        const int q = warp & 3;                        // TMEM lane quarter
+        const int part = (warp - 2) >> 2;              // which kCols of a phase's 128 columns
+        const int c0 = part * kCols;
         const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16);
         // the accumulators start at zero (every MMA accumulates)
-#pragma unroll 1
-        for (int u0 = half * (kU / 2); u0 < (half + 1) * (kU / 2); u0 += 16)
+#pragma unroll
+        for (int gi = 0; gi < kGrp; ++gi)
 #pragma unroll
             for (int a = 0; a < 2; ++a)
 #pragma unroll
-                for (int l = 0; l < kPhT; ++l) tmem_zero16(tq + a * kCrossCol + l * kU + u0);
+                for (int l = 0; l < kPhT; ++l)
+                    tmem_zero16(tq + a * kCrossCol + l * kU + c0 + 16 * gi);
         tmem_wait_st();
         tc_fence_before();
         mbar_arrive(tempty);
@@ -343,41 +348,51 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
             const int64_t row = cg * kM + q * 32 + lane;
             const int64_t o0 = blk * kNCOL + kPhT * pg;
             float* __restrict__ yr = y + row * ld_y;
-#pragma unroll 1
-            for (int u0 = half * (kU / 2); u0 < (half + 1) * (kU / 2); u0 += 16) {
-                float vm[kPhT][16], vc[kPhT][16];
+            // every column of this warp into registers (the two accumulators
+            // summed), TMEM zeroed and handed back, then the global stores:
+            // the next tile's MMAs run while this tile's outputs are written
+            float out[kGrp][kPhT][16];
+#pragma unroll
+            for (int gi = 0; gi < kGrp; ++gi) {
+                const int u0 = c0 + 16 * gi;
 #pragma unroll
                 for (int l = 0; l < kPhT; ++l) {
-                    tmem_ld16(tq + l * kU + u0, vm[l]);
-                    tmem_ld16(tq + kCrossCol + l * kU + u0, vc[l]);
+                    float vc[16];
+                    tmem_ld16(tq + l * kU + u0, out[gi][l]);
+                    tmem_ld16(tq + kCrossCol + l * kU + u0, vc);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) out[gi][l][i] += vc[i];
                 }
-                tmem_wait_ld();
 #pragma unroll
                 for (int a = 0; a < 2; ++a)
 #pragma unroll
                     for (int l = 0; l < kPhT; ++l) tmem_zero16(tq + a * kCrossCol + l * kU + u0);
-                if (row < g.batch) {
+            }
+            tmem_wait_st();
+            tc_fence_before();
+            mbar_arrive(tempty);
+            if (row < g.batch) {
+#pragma unroll
+                for (int gi = 0; gi < kGrp; ++gi) {
                     // column u0 + i holds output ob - 8i (and the next one)
-                    const int64_t ob = o0 + 8 * (kU - 1 - u0);
+                    const int64_t ob = o0 + 8 * (kU - 1 - (c0 + 16 * gi));
                     if (g.vec_store && ob + kPhT <= g.n_out) {
 #pragma unroll
                         for (int i = 0; i < 16; ++i)
                             *reinterpret_cast<float2*>(yr + ob - 8 * i) =
-                                make_float2(vm[0][i] + vc[0][i], vm[1][i] + vc[1][i]);
+                                make_float2(out[gi][0][i], out[gi][1][i]);
                     } else {
 #pragma unroll
                         for (int i = 0; i < 16; ++i)
 #pragma unroll
                             for (int l = 0; l < kPhT; ++l) {
                                 const int64_t o = ob - 8 * i + l;
-                                if (o < g.n_out) yr[o] = vm[l][i] + vc[l][i];
+                                if (o < g.n_out) yr[o] = out[gi][l][i];
                             }
                     }
                 }
             }
-            tmem_wait_st();
-            tc_fence_before();
-            mbar_arrive(tempty);
         }
     }
     __syncthreads();
