@@ -540,6 +540,13 @@ static int sosfilt_impl(const T* x, int64_t ld_x, int64_t batch, int64_t n, cons
     const DeviceInfo* info = nullptr;
     rc = current_device(&info);
     if (rc) return rc;
+    // few long channels: the block-parallel time scan
+    const bool overlap = (const void*)y < (const void*)(x + batch * ld_x) &&
+                         (const void*)x < (const void*)(y + batch * ld_y);
+    const int64_t nb = sos_scan_blocks(batch, n, nsec, precision, overlap);
+    if (nb > 0)
+        return sosfilt_blocked<T>(x, ld_x, batch, n, c, zi, zf, precision, y, ld_y, nb,
+                                  as_stream(stream));
     return launch_sosfilt<T>(x, ld_x, batch, n, c, zi, zf, precision, y, ld_y, as_stream(stream));
 }
 

@@ -80,14 +80,27 @@ struct SosCoef {
 int build_sos_coef(const double* sos, int nsec, bool want_zi, SosCoef* c);
 // FP32-state SOS (FP32, FP32_COUPLED) on f32 data: the cascade split over
 // the warps of a CTA (sos_pipe.cu).
+// blk_rows > 0 (sosfilt only) selects a blocked row view: row r is block
+// r mod blk_rows, of blk_len samples at stride blk_len, of channel
+// r div blk_rows (x and y rows ld_x / ld_y apart); blk_rows must be a
+// multiple of 64.
 int launch_sos_pipe(const float* x, int64_t ld_x, int64_t batch, int64_t n, const SosCoef& c,
                     const double* zi, double* zf, bool filtfilt, int64_t edge, int use_zi,
-                    int precision, float* y, int64_t ld_y, float* tail, cudaStream_t st);
+                    int precision, float* y, int64_t ld_y, float* tail, cudaStream_t st,
+                    int64_t blk_rows = 0, int64_t blk_len = 0);
 
 template <typename T>
 int launch_sosfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const SosCoef& c,
                    const double* zi, double* zf, int precision, T* y, int64_t ld_y,
-                   cudaStream_t st);
+                   cudaStream_t st, int64_t blk_rows = 0, int64_t blk_len = 0);
+// Block-parallel time scan for few long channels (sos_scan.cu): the blocks
+// per channel to cut the signal into (a multiple of 64), or 0 when the
+// request should take the channel-parallel kernels as it is.
+int64_t sos_scan_blocks(int64_t batch, int64_t n, int nsec, int precision, bool in_place);
+template <typename T>
+int sosfilt_blocked(const T* x, int64_t ld_x, int64_t batch, int64_t n, const SosCoef& c,
+                    const double* zi, double* zf, int precision, T* y, int64_t ld_y, int64_t nb,
+                    cudaStream_t st);
 template <typename T>
 int launch_sosfiltfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const SosCoef& c,
                        int64_t edge, int use_zi, int precision, T* y, int64_t ld_y,

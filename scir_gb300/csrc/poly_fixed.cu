@@ -15,10 +15,14 @@
 // of every warp takes period j, so all lanes of a warp sit at the same
 // output phase and use the same taps; warp w takes output positions
 // [20w, 20w + 20) of each period (eight code variants, two per scheduler).
-// The taps live in the kernel-parameter (constant) bank, so each
-// multiply-add reads its tap straight from there: per output only its 20 or
-// 21 FMAs, no tap loads.  The item's 4,724 input samples are staged in
-// shared memory by one bulk copy (4-stage ring); lane j reads sample
+// The taps arrive as kernel parameters, already ordered per warp as they are
+// used (warp w, tap q, position i), and are copied once into shared memory;
+// a warp reads four of its taps with one broadcast 16-byte load (the same
+// address for all lanes), so each output costs its 20 or 21 FMAs plus a
+// quarter load per tap.  (Reading them as constant-bank operands was
+// measured 25x slower: the 13 KB tap set does not fit the constant cache.)
+// The item's 4,724 input samples are staged in shared memory by one bulk
+// copy (3-stage ring); lane j reads sample
 // 147 j + c, and 147 is odd, so the 32 lanes hit 32 different banks.  Each
 // lane keeps the ~40-sample window of its 20 outputs in registers, stores
 // its outputs as 16-byte words into a padded output buffer (two, ping-pong),
@@ -41,12 +45,12 @@ constexpr int kPos = kUp / kNW;                   // output positions per warp
 constexpr int kPer = 32;                          // periods per item (one per lane)
 constexpr int kInSpan = kDown * (kPer - 1) + (kOffM + kDown * (kUp - 1)) / kUp + kQ;  // 4,724
 constexpr int kInStage = (kInSpan + 3 + 3) / 4 * 4 + 8;  // samples per stage, 4-aligned start
-constexpr int kStages = 4;
+constexpr int kStages = 3;
 constexpr int kRowP = kUp + 4;                    // output buffer row (period) stride, floats
 constexpr int kThreads = kNW * 32;
 
 struct FixedTaps {
-    float h[kUp * kQ];  // h[ph + 160 q]; zero where ph + 160 q >= kh
+    float h[kNW * kQ * kPos];  // [warp w][tap q][position i] = h[ph(20w + i) + 160 q], 0 past kh
 };
 
 struct FixedGeom {
@@ -61,8 +65,9 @@ __host__ __device__ constexpr int db_of(int p) { return (kOffM + kDown * p) / kU
 // Outputs [20W, 20W + 20) of the lane's period: the lane's window starts at
 // stage index `w0` (= delta + 147 j + db(20W)).
 template <int W>
-__device__ __forceinline__ void compute_positions(const FixedTaps& T, const float* __restrict__ stage,
-                                                  int w0, float* __restrict__ yrow) {
+__device__ __forceinline__ void compute_positions(const float* __restrict__ taps,
+                                                  const float* __restrict__ stage, int w0,
+                                                  float* __restrict__ yrow) {
     constexpr int P0 = kPos * W;
     constexpr int D0 = db_of(P0);
     constexpr int WN = db_of(P0 + kPos - 1) - D0 + kQ;
@@ -74,11 +79,21 @@ __device__ __forceinline__ void compute_positions(const FixedTaps& T, const floa
     for (int i = 0; i < kPos; ++i) acc[i] = 0.0f;
 #pragma unroll
     for (int q = 0; q < kQ; ++q) {
+        const float4* t4 = reinterpret_cast<const float4*>(taps + (W * kQ + q) * kPos);
 #pragma unroll
-        for (int i = 0; i < kPos; ++i) {
-            const int p = P0 + i;
-            const int hi = ph_of(p) + kUp * q;
-            if (hi < kKh) acc[i] = fmaf(T.h[hi], win[db_of(p) - D0 + kQ - 1 - q], acc[i]);
+        for (int i4 = 0; i4 < kPos / 4; ++i4) {
+            // a group whose taps are all past kh is skipped at compile time
+            if (ph_of(P0 + 4 * i4 + 3) + kUp * q >= kKh && ph_of(P0 + 4 * i4) + kUp * q >= kKh &&
+                ph_of(P0 + 4 * i4 + 1) + kUp * q >= kKh && ph_of(P0 + 4 * i4 + 2) + kUp * q >= kKh)
+                continue;
+            const float4 tv = t4[i4];
+            const float t[4] = {tv.x, tv.y, tv.z, tv.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int p = P0 + 4 * i4 + e;
+                if (ph_of(p) + kUp * q < kKh)
+                    acc[4 * i4 + e] = fmaf(t[e], win[db_of(p) - D0 + kQ - 1 - q], acc[4 * i4 + e]);
+            }
         }
     }
 #pragma unroll
@@ -92,7 +107,8 @@ poly_fixed_kernel(const __grid_constant__ FixedTaps T, const __grid_constant__ F
     extern __shared__ __align__(128) float smem[];
     float* stages = smem;                                  // [kStages][kInStage]
     float* ybuf = stages + kStages * kInStage;             // [2][kPer][kRowP]
-    uint64_t* full = reinterpret_cast<uint64_t*>(ybuf + 2 * kPer * kRowP);
+    float* taps = ybuf + 2 * kPer * kRowP;                 // [kNW][kQ][kPos]
+    uint64_t* full = reinterpret_cast<uint64_t*>(taps + kNW * kQ * kPos);
     __shared__ int delta_s[kStages];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -100,6 +116,7 @@ poly_fixed_kernel(const __grid_constant__ FixedTaps T, const __grid_constant__ F
         for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
         fence_barrier_init();
     }
+    for (int i = tid; i < kNW * kQ * kPos; i += kThreads) taps[i] = T.h[i];
     __syncthreads();
 
     // Loads item `item` into stage s (warp 0): samples [s0, s0 + kInStage)
@@ -160,14 +177,14 @@ poly_fixed_kernel(const __grid_constant__ FixedTaps T, const __grid_constant__ F
         float* yrow = yb + lane * kRowP;
         const int w0 = delta + kDown * lane;
         switch (warp) {
-        case 0: compute_positions<0>(T, st, w0 + db_of(0 * kPos), yrow); break;
-        case 1: compute_positions<1>(T, st, w0 + db_of(1 * kPos), yrow); break;
-        case 2: compute_positions<2>(T, st, w0 + db_of(2 * kPos), yrow); break;
-        case 3: compute_positions<3>(T, st, w0 + db_of(3 * kPos), yrow); break;
-        case 4: compute_positions<4>(T, st, w0 + db_of(4 * kPos), yrow); break;
-        case 5: compute_positions<5>(T, st, w0 + db_of(5 * kPos), yrow); break;
-        case 6: compute_positions<6>(T, st, w0 + db_of(6 * kPos), yrow); break;
-        default: compute_positions<7>(T, st, w0 + db_of(7 * kPos), yrow); break;
+        case 0: compute_positions<0>(taps, st, w0 + db_of(0 * kPos), yrow); break;
+        case 1: compute_positions<1>(taps, st, w0 + db_of(1 * kPos), yrow); break;
+        case 2: compute_positions<2>(taps, st, w0 + db_of(2 * kPos), yrow); break;
+        case 3: compute_positions<3>(taps, st, w0 + db_of(3 * kPos), yrow); break;
+        case 4: compute_positions<4>(taps, st, w0 + db_of(4 * kPos), yrow); break;
+        case 5: compute_positions<5>(taps, st, w0 + db_of(5 * kPos), yrow); break;
+        case 6: compute_positions<6>(taps, st, w0 + db_of(6 * kPos), yrow); break;
+        default: compute_positions<7>(taps, st, w0 + db_of(7 * kPos), yrow); break;
         }
         fence_proxy_async_smem();
         // the output copies of the item before (the other buffer) have
@@ -225,7 +242,12 @@ int launch_poly_fixed(const PolyArgs& a, const float* h_host, cudaStream_t st) {
     unsigned* err = device_error_word();
     if (!err) return set_error(SCIR_ERR_CUDA, "device error word unavailable");
     FixedTaps T;
-    for (int i = 0; i < kUp * kQ; ++i) T.h[i] = i < kKh ? h_host[i] : 0.0f;
+    for (int w = 0; w < kNW; ++w)
+        for (int q = 0; q < kQ; ++q)
+            for (int i = 0; i < kPos; ++i) {
+                const int hi = ph_of(kPos * w + i) + kUp * q;
+                T.h[(w * kQ + q) * kPos + i] = hi < kKh ? h_host[hi] : 0.0f;
+            }
     FixedGeom g;
     g.n = a.n;
     g.ld_x = a.ld_x;
@@ -236,7 +258,8 @@ int launch_poly_fixed(const PolyArgs& a, const float* h_host, cudaStream_t st) {
     const int64_t periods = ceil_div(a.n_out, kUp);
     g.blocks_per_row = ceil_div(periods, kPer);
     g.n_items = g.blocks_per_row * a.batch;
-    const size_t smem = sizeof(float) * ((size_t)kStages * kInStage + 2 * kPer * kRowP) +
+    const size_t smem = sizeof(float) * ((size_t)kStages * kInStage + 2 * kPer * kRowP +
+                                         kNW * kQ * kPos) +
                         kStages * sizeof(uint64_t);
     SCIR_CUDA_TRY(cudaFuncSetAttribute(poly_fixed_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -59,12 +59,24 @@ __global__ void __launch_bounds__(32)
 sosfilt_kernel(const T* __restrict__ x, int64_t ld_x, int64_t batch, int64_t n,
                const __grid_constant__ SosCoef sc,
                const double* __restrict__ zi, double* __restrict__ zf, T* __restrict__ y,
-               int64_t ld_y) {
+               int64_t ld_y, int64_t blk_rows, int64_t blk_len) {
     using A = typename AccT<PREC>::type;
     __shared__ T s[kTT][kTT + 1];
     const int lane = threadIdx.x;
     const int64_t r0 = (int64_t)blockIdx.x * kTT;
     const int64_t ch = r0 + lane;
+    // blocked row view (blk_rows > 0): row r is block r mod blk_rows, of
+    // blk_len samples, of channel r div blk_rows; blk_rows is a multiple of
+    // 32, so the warp's rows lie in one channel at stride blk_len
+    if (blk_rows > 0) {
+        x += (r0 / blk_rows) * ld_x + (r0 % blk_rows) * blk_len;
+        y += (r0 / blk_rows) * ld_y + (r0 % blk_rows) * blk_len;
+        ld_x = ld_y = blk_len;
+    } else {
+        x += r0 * ld_x;
+        y += r0 * ld_y;
+    }
+    const int64_t rows = batch - r0;  // rows of this warp that exist (may exceed 32)
     A s1[NS], s2[NS];
 #pragma unroll
     for (int k = 0; k < NS; ++k) {
@@ -75,19 +87,19 @@ sosfilt_kernel(const T* __restrict__ x, int64_t ld_x, int64_t batch, int64_t n,
                            s1[k], s2[k]);
     }
     T nxt[kTT];
-    tile_fetch(nxt, x, ld_x, r0, batch, n, 0, lane);
+    tile_fetch(nxt, x, ld_x, 0, rows, n, 0, lane);
     for (int64_t t0 = 0; t0 < n; t0 += kTT) {
 #pragma unroll
         for (int i = 0; i < kTT; ++i) s[i][lane] = nxt[i];
         __syncwarp();
-        if (t0 + kTT < n) tile_fetch(nxt, x, ld_x, r0, batch, n, t0 + kTT, lane);
+        if (t0 + kTT < n) tile_fetch(nxt, x, ld_x, 0, rows, n, t0 + kTT, lane);
         const int tn = (int)((n - t0) < kTT ? (n - t0) : kTT);
         for (int t = 0; t < tn; ++t) {
             const A v = sos_step<NS, PREC>(sc, s1, s2, (A)s[lane][t]);
             s[lane][t] = (T)v;
         }
         __syncwarp();
-        tile_store(s, y, ld_y, r0, batch, n, t0, lane);
+        tile_store(s, y, ld_y, 0, rows, n, t0, lane);
         __syncwarp();
     }
     if (zf && ch < batch) {
@@ -199,9 +211,11 @@ sosfiltfilt_kernel(const T* __restrict__ x, int64_t ld_x, int64_t batch, int64_t
 
 template <typename T, int NS, int PREC>
 int run_sosfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const SosCoef& c,
-                const double* zi, double* zf, T* y, int64_t ld_y, cudaStream_t st) {
+                const double* zi, double* zf, T* y, int64_t ld_y, cudaStream_t st,
+                int64_t blk_rows, int64_t blk_len) {
     const int64_t grid = ceil_div(batch, kTT);
-    sosfilt_kernel<T, NS, PREC><<<(unsigned)grid, kTT, 0, st>>>(x, ld_x, batch, n, c, zi, zf, y, ld_y);
+    sosfilt_kernel<T, NS, PREC><<<(unsigned)grid, kTT, 0, st>>>(x, ld_x, batch, n, c, zi, zf, y, ld_y,
+                                                               blk_rows, blk_len);
     SCIR_LAUNCH_CHECK("sosfilt_kernel");
     return SCIR_OK;
 }
@@ -221,9 +235,12 @@ int run_sosfiltfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const So
 
 template <typename T, int PREC>
 int dispatch_sosfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const SosCoef& c,
-                     const double* zi, double* zf, T* y, int64_t ld_y, cudaStream_t st) {
-#define SCIR_CASE(NS) \
-    if (c.nsec <= NS) return run_sosfilt<T, NS, PREC>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st);
+                     const double* zi, double* zf, T* y, int64_t ld_y, cudaStream_t st,
+                     int64_t blk_rows, int64_t blk_len) {
+#define SCIR_CASE(NS)                                                                          \
+    if (c.nsec <= NS)                                                                          \
+        return run_sosfilt<T, NS, PREC>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st, blk_rows, \
+                                        blk_len);
     SCIR_SOS_NS_LIST(SCIR_CASE)
 #undef SCIR_CASE
     return set_error(SCIR_ERR_UNSUPPORTED, "more than %d sections", SCIR_SOS_MAX_SECTIONS);
@@ -245,18 +262,20 @@ int dispatch_sosfiltfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, con
 template <typename T>
 int launch_sosfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const SosCoef& c,
                    const double* zi, double* zf, int precision, T* y, int64_t ld_y,
-                   cudaStream_t st) {
+                   cudaStream_t st, int64_t blk_rows, int64_t blk_len) {
     if (batch == 0) return SCIR_OK;
     if constexpr (std::is_same<T, float>::value)
         if (precision == SCIR_SOS_FP32 || precision == SCIR_SOS_FP32_COUPLED)
             return launch_sos_pipe(x, ld_x, batch, n, c, zi, zf, false, 0, 0, precision, y, ld_y,
-                                   nullptr, st);
+                                   nullptr, st, blk_rows, blk_len);
+    const int64_t br = blk_rows, bl = blk_len;
     switch (precision) {
-    case SCIR_SOS_FP64_EXACT: return dispatch_sosfilt<T, 0>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st);
-    case SCIR_SOS_FP64: return dispatch_sosfilt<T, 1>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st);
-    case SCIR_SOS_FP32: return dispatch_sosfilt<T, 2>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st);
+    case SCIR_SOS_FP64_EXACT:
+        return dispatch_sosfilt<T, 0>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st, br, bl);
+    case SCIR_SOS_FP64: return dispatch_sosfilt<T, 1>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st, br, bl);
+    case SCIR_SOS_FP32: return dispatch_sosfilt<T, 2>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st, br, bl);
     case SCIR_SOS_FP32_COUPLED:
-        return dispatch_sosfilt<T, 3>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st);
+        return dispatch_sosfilt<T, 3>(x, ld_x, batch, n, c, zi, zf, y, ld_y, st, br, bl);
     default: return set_error(SCIR_ERR_INVALID_ARG, "unknown SOS precision %d", precision);
     }
 }
@@ -284,9 +303,11 @@ int launch_sosfiltfilt(const T* x, int64_t ld_x, int64_t batch, int64_t n, const
 }
 
 template int launch_sosfilt<float>(const float*, int64_t, int64_t, int64_t, const SosCoef&,
-                                   const double*, double*, int, float*, int64_t, cudaStream_t);
+                                   const double*, double*, int, float*, int64_t, cudaStream_t,
+                                   int64_t, int64_t);
 template int launch_sosfilt<double>(const double*, int64_t, int64_t, int64_t, const SosCoef&,
-                                    const double*, double*, int, double*, int64_t, cudaStream_t);
+                                    const double*, double*, int, double*, int64_t, cudaStream_t,
+                                    int64_t, int64_t);
 template int launch_sosfiltfilt<float>(const float*, int64_t, int64_t, int64_t, const SosCoef&,
                                        int64_t, int, int, float*, int64_t, float*, cudaStream_t);
 template int launch_sosfiltfilt<double>(const double*, int64_t, int64_t, int64_t, const SosCoef&,

@@ -140,6 +140,7 @@ struct PipeArgs {
     float* tail;       // sosfiltfilt: [edge][batch]
     int use_zi;        // sosfiltfilt: odd padding with sosfilt_zi
     unsigned* err;
+    int64_t blk_rows, blk_len;  // sosfilt: blocked row view (0: plain rows)
 };
 
 template <int NS, int PREC, bool FF>
@@ -157,6 +158,13 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
     const int64_t ch[2] = {r0 + lane, r0 + kTT + lane};
     const bool live[2] = {ch[0] < a.batch, ch[1] < a.batch};
     const int64_t n = a.n, edge = a.edge;
+    // memory rows of this CTA: row r0 + i at x0 + i * ldx (the blocked view
+    // keeps the CTA's 64 rows inside one channel at stride blk_len)
+    const int64_t ldx = a.blk_rows ? a.blk_len : a.ld_x, ldy = a.blk_rows ? a.blk_len : a.ld_y;
+    const float* const x0 =
+        a.x + (a.blk_rows ? (r0 / a.blk_rows) * a.ld_x + (r0 % a.blk_rows) * a.blk_len : r0 * a.ld_x);
+    float* const y0 =
+        a.y + (a.blk_rows ? (r0 / a.blk_rows) * a.ld_y + (r0 % a.blk_rows) * a.blk_len : r0 * a.ld_y);
 
     if (threadIdx.x == 0) {
         for (int w = 0; w < G; ++w)
@@ -257,9 +265,9 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
         float(*t)[kLd] = tiles[slot];
         const bool rows_full = r0 + kCH <= a.batch;
         if (KIND == kSos && rows_full && j0 + kTT <= L) {
-            const float* p = a.x + r0 * a.ld_x + j;
+            const float* p = x0 + j;
 #pragma unroll 8
-            for (int i = 0; i < kCH; ++i, p += a.ld_x) cp_async4(&t[i][lane], p, true);
+            for (int i = 0; i < kCH; ++i, p += ldx) cp_async4(&t[i][lane], p, true);
         } else if (KIND == kFwd && rows_full && j0 >= edge && j0 + kTT <= edge + n) {
             const float* p = a.x + r0 * a.ld_x + (j - edge);
 #pragma unroll 8
@@ -274,7 +282,7 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
                 const bool vr = row < a.batch && j < L;
                 const float* rx = a.x + (row < a.batch ? row : 0) * a.ld_x;
                 if (KIND == kSos) {
-                    cp_async4(&t[i][lane], vr ? rx + j : a.x, vr);
+                    cp_async4(&t[i][lane], vr ? x0 + i * ldx + j : a.x, vr);
                 } else if (KIND == kFwd) {
                     if (j >= edge && j < edge + n) {
                         cp_async4(&t[i][lane], vr ? rx + (j - edge) : a.x, vr);
@@ -304,14 +312,14 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
         float(*t)[kLd] = tiles[slot];
         const bool rows_full = r0 + kCH <= a.batch;
         float* q = nullptr;
-        if (KIND == kSos && rows_full && j0 + kTT <= L) q = a.y + r0 * a.ld_y + j;
+        if (KIND == kSos && rows_full && j0 + kTT <= L) q = y0 + j;
         if (KIND == kFwd && rows_full && j0 >= edge && j0 + kTT <= edge + n)
             q = a.y + r0 * a.ld_y + (j - edge);
         if (KIND == kBwd && rows_full && j0 >= edge && j0 + kTT <= L)
             q = a.y + r0 * a.ld_y + (n - 1 - (j - edge));
         if (q) {
 #pragma unroll 8
-            for (int i = 0; i < kCH; ++i, q += a.ld_y) *q = t[i][lane];
+            for (int i = 0; i < kCH; ++i, q += (KIND == kSos ? ldy : a.ld_y)) *q = t[i][lane];
             // the forward stream's last output seeds the backward pass (edge == 0)
             if (KIND == kFwd && j == L - 1)
                 for (int i = 0; i < kCH; ++i) ylast_s[i] = t[i][lane];
@@ -323,7 +331,7 @@ sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
             const float v = t[i][lane];
             float* ry = a.y + row * a.ld_y;
             if (KIND == kSos) {
-                ry[j] = v;
+                y0[(row - r0) * ldy + j] = v;
             } else if (KIND == kFwd) {
                 if (j >= edge && j < edge + n) ry[j - edge] = v;
                 else if (j >= edge + n) a.tail[(j - edge - n) * a.batch + row] = v;
@@ -456,11 +464,14 @@ int dispatch_pipe(const SosCoef& c, const PipeArgs& a, cudaStream_t st) {
 
 int launch_sos_pipe(const float* x, int64_t ld_x, int64_t batch, int64_t n, const SosCoef& c,
                     const double* zi, double* zf, bool filtfilt, int64_t edge, int use_zi,
-                    int precision, float* y, int64_t ld_y, float* tail, cudaStream_t st) {
+                    int precision, float* y, int64_t ld_y, float* tail, cudaStream_t st,
+                    int64_t blk_rows, int64_t blk_len) {
     if (batch == 0 || n == 0) return SCIR_OK;
+    SCIR_REQUIRE(blk_rows == 0 || (!filtfilt && blk_rows % kCH == 0), SCIR_ERR_INVALID_ARG,
+                 "blocked rows need sosfilt and a multiple of %d blocks per channel", kCH);
     unsigned* err = device_error_word();
     if (!err) return set_error(SCIR_ERR_CUDA, "device error word unavailable");
-    PipeArgs a{x, ld_x, y, ld_y, batch, n, edge, zi, zf, tail, use_zi, err};
+    PipeArgs a{x, ld_x, y, ld_y, batch, n, edge, zi, zf, tail, use_zi, err, blk_rows, blk_len};
     const bool coupled = precision == SCIR_SOS_FP32_COUPLED;
     if (filtfilt) return coupled ? dispatch_pipe<3, true>(c, a, st) : dispatch_pipe<2, true>(c, a, st);
     return coupled ? dispatch_pipe<3, false>(c, a, st) : dispatch_pipe<2, false>(c, a, st);

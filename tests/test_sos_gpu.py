@@ -222,3 +222,52 @@ def test_fp32_pipe_channel_halves(cuda, batch):
     ydf = S.sosfilt_f32(SOS5, _dev(x, cuda), precision=S.SosPrecision.FP32).cpu().numpy()
     assert np.all(np.isfinite(ydf))
     del torch
+
+
+# ----------------------------------------- block-parallel time scan (few, long channels)
+# Up to 64 channels of long signals are cut into blocks filtered from zero
+# state, the block states are chained by a scan with the cascade's L-step
+# transition matrix, and every block is filtered again from its true state.
+# FP32-state modes keep their 1e-5 bound; FP64 state takes the path with
+# blocks of >= 65,536 samples and a stated bound of 1e-9; FP64_EXACT stays
+# sequential (bit-identical to the reference order).
+@pytest.mark.parametrize("batch,n", [(1, 1 << 20), (2, 3_000_017), (5, 700_001)])
+def test_block_scan_fp32_coupled(cuda, batch, n):
+    rng = np.random.default_rng(batch + n)
+    x = rng.standard_normal((batch, n)).astype(np.float32)
+    x64 = x.astype(np.float64)
+    P = S.SosPrecision.FP32_COUPLED
+    zi = rng.standard_normal((batch, 8, 2)) * 0.01
+    y, zf = S.sosfilt_f32(SOS5, _dev(x, cuda), zi=_dev(zi, cuda), return_zf=True, precision=P)
+    ref, ref_zf = O.sosfilt_f64(SOS5, x64, zi=zi, return_zf=True)
+    assert normwise_err(y.cpu().numpy(), ref) < TOL
+    assert np.max(np.abs(zf.cpu().numpy() - ref_zf)) < 1e-4 * np.max(np.abs(ref_zf))
+    # chained: the second half continues from the first half's final state
+    h = n // 2
+    y1, z1 = S.sosfilt_f32(SOS5, _dev(x[:, :h], cuda), return_zf=True, precision=P)
+    y2 = S.sosfilt_f32(SOS5, _dev(x[:, h:], cuda), zi=z1, precision=P)
+    full = np.concatenate([y1.cpu().numpy(), y2.cpu().numpy()], 1)
+    assert normwise_err(full, O.sosfilt_f64(SOS5, x64)) < TOL
+
+
+def test_block_scan_fp64_state(cuda):
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal((2, 9_000_000)).astype(np.float32)
+    ref = O.sosfilt_f64(SOS5, x.astype(np.float64))
+    y = S.sosfilt_f32(SOS5, _dev(x, cuda), precision=S.SosPrecision.FP64).cpu().numpy()
+    assert normwise_err(y, ref) < 1e-6  # f32 outputs: their rounding dominates
+    # f64 data, FP64 state: the scan's own bound
+    xd = rng.standard_normal((1, 5_000_000))
+    yd = S.sosfilt_f64(SOS5, _dev(xd, cuda), precision=S.SosPrecision.FP64).cpu().numpy()
+    assert normwise_err(yd, O.sosfilt_f64(SOS5, xd)) < 1e-9
+
+
+def test_block_scan_exact_and_in_place_stay_sequential(cuda):
+    rng = np.random.default_rng(12)
+    xd = rng.standard_normal((1, 2_000_000))
+    y = S.sosfilt_f64(SOS5, _dev(xd, cuda), precision=S.SosPrecision.FP64_EXACT).cpu().numpy()
+    assert np.array_equal(y, O.sosfilt_f64(SOS5, xd))  # the reference order, bit for bit
+    x = rng.standard_normal((1, 1 << 20)).astype(np.float32)
+    xg = _dev(x, cuda)
+    S.sosfilt_f32(SOS5, xg, precision=S.SosPrecision.FP32_COUPLED, out=xg)  # in place
+    assert normwise_err(xg.cpu().numpy(), O.sosfilt_f64(SOS5, x.astype(np.float64))) < TOL
