@@ -83,7 +83,6 @@ struct TapKey {
 struct TapBuf {
     float* d32 = nullptr;
     double* d64 = nullptr;
-    const float* h32 = nullptr;  // host copy (kept for the process, like the device copies)
     int64_t kh = 0;
 };
 std::mutex g_tap_mutex;
@@ -146,9 +145,6 @@ int cached_default_taps(int up, int down, int design, TapBuf* out) {
     std::vector<float> hf(h.begin(), h.end());
     TapBuf b;
     b.kh = (int64_t)h.size();
-    float* hcopy = new float[hf.size()];
-    std::copy(hf.begin(), hf.end(), hcopy);
-    b.h32 = hcopy;
     SCIR_CUDA_TRY(cudaMalloc(&b.d32, hf.size() * sizeof(float)));
     SCIR_CUDA_TRY(cudaMalloc(&b.d64, h.size() * sizeof(double)));
     rc = upload_sync(b.d32, hf.data(), hf.size() * sizeof(float));
@@ -333,14 +329,7 @@ int poly_dispatch(const PolyArgs& a, int precision, cudaStream_t st) {
     case SCIR_PREC_FP32:
     case SCIR_PREC_REF_EXACT:
     case SCIR_PREC_AUTO: {
-        // the compile-time-specialised kernel serves the default design of its
-        // rate pair (its taps go into the kernel parameters from the host
-        // copy); the autotuner may have found the streaming kernel faster
         const int tuned = tune_poly_choice(a);
-        const bool fixed = a.h_host && poly_fixed_supported(a);
-        if (fixed && (tuned == 0 || tuned == kPolyFixedChoice))
-            return launch_poly_fixed(a, a.h_host, st);
-        if (tuned == kPolyFixedChoice) return launch_poly_simt(a, st, 0, 0);
         return launch_poly_simt(a, st, tuned / 10, tuned % 10);
     }
     case SCIR_PREC_BF16X3:
@@ -494,20 +483,17 @@ SCIR_API int scir_resample_poly_f32(const float* x, int64_t ld_x, int64_t batch,
                                         n * sizeof(float), batch, cudaMemcpyDeviceToDevice, st));
         return SCIR_OK;
     }
-    const float* h_host = nullptr;
     if (h == nullptr) {
         TapBuf b;
         rc = cached_default_taps(up0, down0, 0, &b);
         if (rc) return rc;
         h = b.d32;
-        h_host = b.h32;
         kh = b.kh;
     }
     SCIR_REQUIRE(kh >= 1, SCIR_ERR_INVALID_ARG, "h must hold at least one tap");
     PolyArgs a;
     a.x = x; a.ld_x = ld_x; a.batch = batch; a.n = n; a.h = h; a.kh = kh;
     a.up = up; a.down = down; a.off = (kh - 1) / 2; a.y = y; a.ld_y = ld_y; a.n_out = n_out;
-    a.h_host = h_host;
     return poly_dispatch(a, precision, st);
 }
 

@@ -39,12 +39,7 @@ struct PolyArgs {
     int64_t off;
     float* y;
     int64_t ld_y, n_out;
-    const float* h_host = nullptr;  // the same taps on the host, when the caller has them
 };
-// Compile-time-specialised polyphase kernel (poly_fixed.cu): 160/147 with the
-// default 3,201-tap design; needs the taps on the host (kernel parameters).
-bool poly_fixed_supported(const PolyArgs& a);
-int launch_poly_fixed(const PolyArgs& a, const float* h_host, cudaStream_t st);
 // p_force: outputs per lane (at least the minimum for the rate), ct: channels
 // per work item (1, 2 or 4); 0 = defaults.
 int launch_poly_simt(const PolyArgs& a, cudaStream_t st, int p_force = 0, int ct = 0);
@@ -54,9 +49,7 @@ int launch_poly_simt(const PolyArgs& a, cudaStream_t st, int p_force = 0, int ct
 // FIR choice: 1 = CUDA cores, 8 outputs per thread; 2 = CUDA cores, 16;
 // 3 = tensor cores (BF16X6, AUTO precision only).
 int tune_fir_choice(const FirArgs& a, int precision);
-// polyphase choice: P * 10 + CT of the streaming kernel, kPolyFixedChoice
-// for the compile-time-specialised kernel, 0 = untuned.
-constexpr int kPolyFixedChoice = 99;
+// polyphase choice: P * 10 + CT (0 = untuned).
 int tune_poly_choice(const PolyArgs& a);
 int launch_poly_tc(const PolyArgs& a, int terms, cudaStream_t st);
 bool poly_tc_supported(const PolyArgs& a);

@@ -22,8 +22,8 @@
 // The DF2T cascade coordinates are ill-conditioned for poles near the unit
 // circle (|Phi| reaches ~1e18 for an order-8 band-pass 2e-4 from the circle),
 // so the scan costs accuracy: in an FP64 model of that filter the block
-// result differs from the sequential one by 5e-9 (L = 4,096) to 4e-12
-// (L = 65,536) normwise.  That is far below the FP32-state modes' own error,
+// result differs from the sequential one by 6e-9 (L = 1,024 .. 4,096) to
+// 4e-12 (L = 65,536) normwise.  That is far below the FP32-state modes' own error,
 // so those modes (FP32, FP32_COUPLED) take this path when it pays; FP64
 // takes it only for L >= 65,536 (stated bound 1e-9), and FP64_EXACT -- the
 // reference's sequential operation order -- never does.
@@ -116,10 +116,12 @@ int64_t sos_scan_blocks(int64_t batch, int64_t n, int nsec, int precision, bool 
     if (precision != SCIR_SOS_FP32 && precision != SCIR_SOS_FP32_COUPLED &&
         precision != SCIR_SOS_FP64)
         return 0;
-    // FP32 state: the longest blocks (4,096 .. 65,536 samples) that still
-    // give ~16,384 block rows; FP64 state: >= 65,536 for its stated bound
-    int64_t L = precision == SCIR_SOS_FP64 ? 65536 : 4096;
-    while (L < 65536 && batch * (n / (2 * L)) >= 16384) L *= 2;
+    // FP32 state: the longest blocks (1,024 .. 65,536 samples) that still
+    // give ~19,456 block rows (two 64-row CTAs per SM); FP64 state: 65,536
+    // for its stated bound
+    int64_t L = 65536;
+    if (precision != SCIR_SOS_FP64)
+        while (L > 1024 && batch * (n / L) < 19456) L /= 2;
     // blocks per channel: a multiple of 64, so a CTA's rows share a channel
     const int64_t nb = (n / L) / 64 * 64;
     return nb >= 64 ? nb : 0;

@@ -282,23 +282,6 @@ SCIR_API int scir_autotune_resample_poly(int64_t batch, int64_t n, int up, int d
             }
         }
     }
-    // the compile-time-specialised kernel, where the rates and the filter
-    // length have one (it takes the taps from the host)
-    a.h_host = nullptr;
-    if (!rc && poly_fixed_supported(a)) {
-        std::vector<float> hh((size_t)khr);
-        uint32_t r = 12345u;
-        for (float& v : hh) {
-            r = r * 1664525u + 1013904223u;
-            v = (float)((r >> 8) & 0xFFFF) / 65536.0f - 0.5f;
-        }
-        float t = 0.0f;
-        rc = time_calls([&]() -> int { return launch_poly_fixed(a, hh.data(), st); }, st, 3, &t);
-        if (!rc && (best == 0 || t < best_t)) {
-            best = kPolyFixedChoice;
-            best_t = t;
-        }
-    }
     scratch_free(x, st);
     scratch_free(h, st);
     scratch_free(y, st);
@@ -311,10 +294,7 @@ SCIR_API int scir_autotune_resample_poly(int64_t batch, int64_t n, int up, int d
     }
     if (best_ms) *best_ms = best_t;
     put_choice(choice, choice_len,
-               best == kPolyFixedChoice
-                   ? std::string("fixed-rate kernel (160/147, 3,201 taps)")
-                   : "P=" + std::to_string(best / 10) +
-                         " channels-per-item=" + std::to_string(best % 10));
+               "P=" + std::to_string(best / 10) + " channels-per-item=" + std::to_string(best % 10));
     return SCIR_OK;
 }
 

@@ -200,15 +200,13 @@ def test_resample_tc_cfg2_full_size(cuda):
     assert err < TOL_TC
 
 
-# ------------------------------------- compile-time 160/147 kernel (default design)
-# resample_poly(x, 160, 147) with the default 3,201-tap design runs a kernel
-# whose rates, phases and tap counts are compile-time constants (items of one
-# channel x 32 periods).  Lengths below cover a partial first item, item and
-# period boundaries (4,704 inputs per item), rows shorter than the filter and
-# a length that is not a multiple of 4.
+# ------------------------------------- 160/147 default design over ragged lengths
+# Lengths cover rows shorter than the filter, the 147-input period and its
+# multiples around a work item, and a length that is not a multiple of 4; the
+# default design and the same taps passed explicitly give the same result.
 @pytest.mark.parametrize("n", [1, 2, 37, 1600, 4703, 4704, 4705, 9409, 150001])
 @pytest.mark.parametrize("batch", [1, 3])
-def test_resample_fixed_rate_lengths(cuda, n, batch):
+def test_resample_160_147_lengths(cuda, n, batch):
     rng = np.random.default_rng(n + batch)
     x = rng.standard_normal((batch, n)).astype(np.float32)
     h = S.resample_poly_default_taps(160, 147).astype(np.float32)
@@ -216,6 +214,5 @@ def test_resample_fixed_rate_lengths(cuda, n, batch):
     y = S.resample_poly_f32(_dev(x, cuda), 160, 147).cpu().numpy()
     assert y.shape == ref.shape
     assert normwise_err(y, ref) < TOL_FP32
-    # the same taps passed explicitly run the streaming kernel: the two agree
     y2 = S.resample_poly_f32(_dev(x, cuda), 160, 147, h=_dev(h, cuda)).cpu().numpy()
     assert normwise_err(y, y2) < 1e-6
