@@ -1083,14 +1083,54 @@ def run_ours(args):
     return 0
 
 
+def copy_ceiling(torch, mib=1024, chunks=(1, 4)):
+    """Pinned host <-> device copy bandwidth in GB/s: one direction at a
+    time and both at once, the buffer split into `chunks` copies on as many
+    streams (the host-buffer entry points overlap copies in both directions
+    with the kernels, so these bound their end-to-end rate)."""
+    n = mib << 18  # floats
+    h_in = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    h_out = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    d_in = torch.empty(n, dtype=torch.float32, device="cuda")
+    d_out = torch.empty(n, dtype=torch.float32, device="cuda")
+    h_in.fill_(1.0)
+    out = {}
+    for c in chunks:
+        streams = [torch.cuda.Stream() for _ in range(c)]
+        step = n // c
+
+        def run(h2d, d2h):
+            for i, st in enumerate(streams):
+                with torch.cuda.stream(st):
+                    sl = slice(i * step, (i + 1) * step)
+                    if h2d:
+                        d_in[sl].copy_(h_in[sl], non_blocking=True)
+                    if d2h:
+                        h_out[sl].copy_(d_out[sl], non_blocking=True)
+
+        for name, h2d, d2h in (("h2d", True, False), ("d2h", False, True), ("both", True, True)):
+            run(h2d, d2h)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(3):
+                run(h2d, d2h)
+            torch.cuda.synchronize()
+            dt = (time.perf_counter() - t0) / 3
+            moved = 4 * n * ((1 if h2d else 0) + (1 if d2h else 0))
+            out[f"{name}_{c}_streams_gbs"] = moved / dt / 1e9
+    return out
+
+
 def run_probe():
     import torch
 
     import scir_gb300 as S
     torch.cuda.set_device(0)
-    line = {"probe": "FMA throughput of the CUDA cores (scir_probe_fma_peak)",
+    line = {"probe": "FMA throughput of the CUDA cores (scir_probe_fma_peak) and pinned "
+                     "host<->device copy bandwidth (1 GiB each way)",
             "fp32_tflops": [S.probe_fma_peak(False) for _ in range(3)],
             "fp64_tflops": [S.probe_fma_peak(True) for _ in range(3)],
+            "copies": copy_ceiling(torch),
             "device": torch.cuda.get_device_name(0)}
     print(json.dumps(line), flush=True)
     return 0
