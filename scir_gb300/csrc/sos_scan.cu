@@ -39,32 +39,63 @@ namespace {
 constexpr int kMaxScanStates = 32;  // 2 x 16 sections
 
 // S_{b+1} = Phi S_b + f_b for one channel per CTA (one warp, lane i holds
-// state component i): f [ch][nb][S] final states of the zero-state blocks,
-// zi [ch][S] or null; writes the states entering every block, sin
-// [ch][nb][S], and the state after the last block, fin [ch][S].
+// state component i; S states): f [ch][nb][S] final states of the
+// zero-state blocks, zi [ch][S] or null; writes the states entering every
+// block, sin [ch][nb][S], and the state after the last block, fin [ch][S].
+// The f values of the next 32 blocks are loaded together, so a step waits
+// only for the shuffles and FMAs of the recurrence itself.
+template <int S>
 __global__ void __launch_bounds__(32)
-sos_block_scan_kernel(const double* __restrict__ phi, int S, const double* __restrict__ f,
+sos_block_scan_kernel(const double* __restrict__ phi, const double* __restrict__ f,
                       const double* __restrict__ zi, int64_t nb, double* __restrict__ sin,
                       double* __restrict__ fin) {
     const int64_t ch = blockIdx.x;
     const int i = threadIdx.x;
-    double prow[kMaxScanStates];
+    const bool on = i < S;
+    double prow[S];
 #pragma unroll
-    for (int j = 0; j < kMaxScanStates; ++j) prow[j] = (i < S && j < S) ? phi[i * S + j] : 0.0;
-    double s = (i < S && zi) ? zi[ch * S + i] : 0.0;
+    for (int j = 0; j < S; ++j) prow[j] = on ? phi[i * S + j] : 0.0;
+    double s = (on && zi) ? zi[ch * S + i] : 0.0;
     const double* fc = f + ch * nb * S;
     double* sc = sin + ch * nb * S;
-    for (int64_t b = 0; b < nb; ++b) {
-        if (i < S) sc[b * S + i] = s;
-        // four partial sums keep the dependent chain short
-        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int64_t b0 = 0; b0 < nb; b0 += 32) {
+        double fb[32];
 #pragma unroll
-        for (int j = 0; j < kMaxScanStates; ++j)
-            acc[j & 3] = fma(prow[j], __shfl_sync(0xffffffffu, s, j), acc[j & 3]);
-        const double fb = i < S ? fc[b * S + i] : 0.0;
-        s = (acc[0] + acc[1]) + (acc[2] + acc[3]) + fb;
+        for (int j = 0; j < 32; ++j) fb[j] = (on && b0 + j < nb) ? fc[(b0 + j) * S + i] : 0.0;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            if (b0 + j >= nb) break;
+            if (on) sc[(b0 + j) * S + i] = s;
+            double acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+            for (int q = 0; q < S; ++q)
+                acc[q & 3] = fma(prow[q], __shfl_sync(0xffffffffu, s, q), acc[q & 3]);
+            s = (acc[0] + acc[1]) + (acc[2] + acc[3]) + fb[j];
+        }
     }
-    if (i < S) fin[ch * S + i] = s;
+    if (on) fin[ch * S + i] = s;
+}
+
+template <int S>
+int launch_scan(const double* phi, const double* f, const double* zi, int64_t batch, int64_t nb,
+                double* sin, double* fin, cudaStream_t st) {
+    sos_block_scan_kernel<S><<<(unsigned)batch, 32, 0, st>>>(phi, f, zi, nb, sin, fin);
+    SCIR_LAUNCH_CHECK("sos_block_scan_kernel");
+    return SCIR_OK;
+}
+
+int scan_dispatch(int S, const double* phi, const double* f, const double* zi, int64_t batch,
+                  int64_t nb, double* sin, double* fin, cudaStream_t st) {
+    switch (S) {
+#define SCIR_SCAN_CASE(N) \
+    case N: return launch_scan<N>(phi, f, zi, batch, nb, sin, fin, st);
+        SCIR_SCAN_CASE(2) SCIR_SCAN_CASE(4) SCIR_SCAN_CASE(6) SCIR_SCAN_CASE(8) SCIR_SCAN_CASE(10)
+        SCIR_SCAN_CASE(12) SCIR_SCAN_CASE(14) SCIR_SCAN_CASE(16) SCIR_SCAN_CASE(18)
+        SCIR_SCAN_CASE(20) SCIR_SCAN_CASE(22) SCIR_SCAN_CASE(24) SCIR_SCAN_CASE(26)
+        SCIR_SCAN_CASE(28) SCIR_SCAN_CASE(30) SCIR_SCAN_CASE(32)
+#undef SCIR_SCAN_CASE
+    default: return set_error(SCIR_ERR_UNSUPPORTED, "block scan with %d states", S);
+    }
 }
 
 // Phi = A^L for the cascade c (DF2T state coordinates, zero input), FP64.
@@ -152,12 +183,7 @@ int sosfilt_blocked(const T* x, int64_t ld_x, int64_t batch, int64_t n, const So
     if (!rc)
         rc = launch_sosfilt<T>(x, ld_x, batch * nb, L, c, nullptr, f, precision, y, ld_y, st, nb, L);
     // 2. the states entering every block
-    if (!rc) {
-        sos_block_scan_kernel<<<(unsigned)batch, 32, 0, st>>>(d_phi, S, f, zi, nb, sin, fin);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess)
-            rc = set_error(SCIR_ERR_CUDA, "sos_block_scan_kernel: %s", cudaGetErrorString(e));
-    }
+    if (!rc) rc = scan_dispatch(S, d_phi, f, zi, batch, nb, sin, fin, st);
     // 3. every block again from its true state; the samples past the last
     //    block from the state after it; the final state
     if (!rc)
