@@ -311,8 +311,8 @@ class FirLong(Workload):
         if precision in (S.Precision.BF16X3, S.Precision.BF16X6, S.Precision.AUTO):
             # operand split (signal, taps) + the two tensor-core passes; the
             # roofline time is the whole step, split kernels included
-            self.kernel = "fir_tc_kernel x2 + split kernels (whole step)"
-            self.launches_per_step = 4
+            self.kernel = "fir_tc_kernel + split kernels (whole step)"
+            self.launches_per_step = 3
             self.roofline_launches = 1
         else:
             self.kernel = "fir_simt_kernel"
@@ -521,13 +521,15 @@ class Ragged(Workload):
     persistent launch (lfilter semantics)."""
     name = "fir_ragged_4096"
     COUNT = 4096
-    bound = "fp32"
+    bound = "mixed"
 
     def __init__(self, torch, dev, precision, channels=None):
         import scipy.signal as ss
         import scir_gb300 as S
         self.S, self.torch, self.dev = S, torch, dev
-        self.precision = S.Precision.FP32 if precision == S.Precision.AUTO else precision
+        # AUTO: signals with long filters on the tensor cores (split-bf16, <= 1e-5),
+        # the rest in FP32 on the CUDA cores
+        self.precision = precision
         count = channels or self.COUNT
         self.n, self.k, cut = self.draw(count)
         taps = np.concatenate([ss.firwin(int(k), c, window="hamming") for k, c in zip(self.k, cut)])
@@ -536,7 +538,8 @@ class Ragged(Workload):
         self.x = torch.rand(int(self.n.sum()), device=dev, generator=g) * 2 - 1
         self.plan = S.RaggedPlan(self.n, self.k, S.FirMode.LFILTER, self.precision)
         self.y = torch.empty(self.plan.y_len, device=dev)
-        self.kernel = "ragged_kernel (one persistent launch, replayed from a CUDA graph)"
+        self.kernel = ("ragged_kernel + fir_tc_kernel (tensor-core bucket), replayed from a "
+                       "CUDA graph")
         self.graph = None
 
     @staticmethod
@@ -562,11 +565,25 @@ class Ragged(Workload):
     def alg_flops(self):
         return 2.0 * self.plan.macs
 
+    def floor_ms(self, fp32_tflops, bf16_tflops):
+        """Time floor of the plan: each signal's multiply-adds at the peak of
+        the unit that runs it (FP32 FMA, or six bf16 products per output on
+        the tensor cores)."""
+        thr, _ = self.plan.tensor_cores()
+        n_out = self.plan.n_out
+        tc = (self.k >= thr) & (n_out >= 16384) if thr else np.zeros(len(self.k), bool)
+        fl = 2.0 * n_out.astype(np.float64) * self.k
+        return 1e3 * (fl[~tc].sum() / (fp32_tflops * 1e12) + 6 * fl[tc].sum() / (bf16_tflops * 1e12))
+
     def prepare(self):
         """Records the plan's launch (work-counter reset + persistent kernel)
         into a CUDA graph once; every step replays it.  Runs after the
         autotuner, which rebuilds the plan's tile table."""
         self.S.init(self.dev.index or 0)
+        # split kernels + tensor-core launch (when the plan has that bucket) + the
+        # CUDA-core launch; the roofline covers the whole step
+        self.launches_per_step = 4 if self.plan.tensor_cores()[1] else 1
+        self.roofline_launches = 1
         self.plan.run(self.x, self.taps, self.y)
         self.torch.cuda.synchronize()
         cs = self.torch.cuda.Stream(self.dev)
@@ -583,7 +600,9 @@ class Ragged(Workload):
 
     def autotune(self):
         thr, ms = self.plan.autotune(self.x, self.taps, self.y)
-        return f"16 outputs per thread from {thr} taps ({ms:.3f} ms)"
+        tc, cnt = self.plan.tensor_cores()
+        return (f"16 outputs per thread from {thr} taps; tensor cores from "
+                f"{tc if tc and tc < (1 << 30) else 'never'} taps ({cnt} signals) ({ms:.3f} ms)")
 
     def per_signal_ms(self, stream):
         """The same work as one scir_fir_batched_f32 launch per signal."""
@@ -902,6 +921,13 @@ def roofline(W, kern_ms, peaks, fma):
     """Roofline of the dominant kernel: the algorithmic work of one launch
     over its mean duration, against the binding peak."""
     rl = getattr(W, "roofline_launches", W.launches_per_step)
+    if W.bound == "mixed":
+        floor = W.floor_ms(fma(False), peaks["bf16_tflops"])
+        return {"bound": "mixed", "achieved": floor, "peak": kern_ms, "unit": "ms (floor vs measured)",
+                "frac": floor / kern_ms, "traffic": profile_traffic(W.name), "kernel": W.kernel,
+                "kernel_ms": kern_ms,
+                "peak_source": "per-signal floor: FP32 FMA peak measured live by scir_probe_fma_peak, "
+                               "bf16 " + peaks["source"]}
     if W.bound == "hbm":
         achieved = W.alg_bytes() / rl / (kern_ms / 1e3) / 1e9
         peak, unit, src = peaks["hbm_gbs"], "GB/s", peaks["source"]

@@ -206,7 +206,11 @@ typedef struct scir_ragged_plan scir_ragged_plan;
 
 /* Builds a launch plan from a HOST descriptor table: validates every entry,
  * splits signals into work tiles, orders them longest-first and uploads the
- * tile table to the device.  `precision` may be SCIR_PREC_AUTO. */
+ * tile table to the device.  Precision: SCIR_PREC_FP32 / REF_EXACT run every
+ * signal on the CUDA cores; SCIR_PREC_AUTO (or BF16X6, BF16X3) sends the
+ * signals with at least 512 taps (autotunable) and 16,384 outputs to the
+ * tensor cores (split-bf16 contraction, three or two terms) in a second
+ * persistent launch, the rest to the CUDA cores in FP32. */
 SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count,
                                      int mode, int precision,
                                      scir_ragged_plan** plan);
@@ -215,8 +219,13 @@ SCIR_API int scir_ragged_plan_destroy(scir_ragged_plan* plan);
 SCIR_API int scir_ragged_plan_stats(const scir_ragged_plan* plan,
                                     int64_t* tiles, double* macs,
                                     int64_t* samples_in);
-/* One persistent launch over every tile of the plan (graph-capturable:
- * no allocation, no host synchronisation). */
+/* The tensor-core bucket of a plan: its tap threshold (0: none) and how
+ * many signals it holds. */
+SCIR_API int scir_ragged_plan_tensor_cores(const scir_ragged_plan* plan, int* min_taps,
+                                           int64_t* signals);
+/* One persistent launch over every CUDA-core tile of the plan, preceded by
+ * the tensor-core bucket's operand split and persistent launch when the plan
+ * has one (graph-capturable: no allocation, no host synchronisation). */
 SCIR_API int scir_fir_ragged_f32(const scir_ragged_plan* plan, const float* x,
                                  const float* taps, float* y, void* stream);
 
@@ -311,9 +320,10 @@ SCIR_API int scir_autotune_fir(int64_t batch, int64_t n, int64_t k, int mode,
 SCIR_API int scir_autotune_resample_poly(int64_t batch, int64_t n, int up,
                                          int down, int64_t kh, double* best_ms,
                                          char* choice, size_t choice_len);
-/* Ragged plan: the tap count from which tiles use 16 outputs per thread,
- * timed on the caller's buffers; the plan's tile list is rebuilt with the
- * fastest (the stream is synchronised first). */
+/* Ragged plan: the tap count from which CUDA-core tiles use 16 outputs per
+ * thread and, for plans with a tensor-core bucket, the tap count from which
+ * signals go to the tensor cores, timed on the caller's buffers; the plan is
+ * rebuilt with the fastest (the stream is synchronised first). */
 SCIR_API int scir_ragged_plan_autotune(scir_ragged_plan* plan, const float* x,
                                        const float* taps, float* y, void* stream,
                                        int* v16_min_taps, double* best_ms);

@@ -728,9 +728,16 @@ class RaggedPlan:
                                           _stream(stream)))
         return y
 
+    def tensor_cores(self):
+        """(tap threshold of the tensor-core bucket or 0, signals in it)."""
+        t, c = ctypes.c_int(), ctypes.c_int64()
+        _check(load().scir_ragged_plan_tensor_cores(self._h, ctypes.byref(t), ctypes.byref(c)))
+        return t.value, c.value
+
     def autotune(self, x, taps, y, stream=None):
-        """Times the tile variants on these buffers and rebuilds the plan with
-        the fastest; returns (16-output tap threshold, ms per launch)."""
+        """Times the tile variants (and, with a tensor-core bucket, its tap
+        threshold) on these buffers and rebuilds the plan with the fastest;
+        returns (16-output tap threshold, ms per launch)."""
         thr = ctypes.c_int()
         ms = ctypes.c_double()
         _check(load().scir_ragged_plan_autotune(self._h, x.data_ptr(), taps.data_ptr(), y.data_ptr(),

@@ -33,6 +33,7 @@ SIGNATURES = {
     "scir_fir_batched_f32": (_int, [_vp, _i64, _i64, _i64, _vp, _i64, _int, _int, _vp, _i64, _vp]),
     "scir_ragged_plan_create": (_int, [_vp, _i64, _int, _int, ctypes.POINTER(_vp)]),
     "scir_ragged_plan_destroy": (_int, [_vp]),
+    "scir_ragged_plan_tensor_cores": (_int, [_vp, ctypes.POINTER(_int), ctypes.POINTER(_i64)]),
     "scir_ragged_plan_stats": (_int, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(ctypes.c_double),
                                       ctypes.POINTER(_i64)]),
     "scir_fir_ragged_f32": (_int, [_vp, _vp, _vp, _vp, _vp]),

@@ -64,6 +64,8 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cstring>
+#include <vector>
 
 namespace scir {
 namespace {
@@ -182,10 +184,77 @@ __device__ __forceinline__ void live_rows(int64_t J0, int64_t L0, int64_t k, int
     if (hi > kU) hi = kU;
 }
 
-template <int T>  // bf16 terms per operand: 2 (BF16X3) or 3 (BF16X6)
+// What one role needs to know about a tile: the signal box (tensor map and
+// coordinates), the filter (tap planes, taps, shift, K chunks), the phase
+// group, and where its outputs go.  Batched launches derive it from the
+// geometry; ragged launches read it from the plan's tile and signal tables.
+struct TileView {
+    const CUtensorMap* map;
+    const __nv_bfloat16* G;
+    int64_t LG, k;
+    int m, nchunks, pg, vec_store;
+    int32_t xc0, row0;   // TMA x coordinate of the first chunk, first row of the box
+    int64_t rows;        // rows of the box that exist
+    float* y;            // output row row0 (rows ld apart)
+    int64_t ld, o0;      // row stride; output index of column 0 of phase 0 inside a row
+    int64_t lim0, dlim;  // outputs past (lim0 - r * dlim) of box row r are not stored
+};
+
+template <bool RAGGED>
+__device__ __forceinline__ TileView tile_view(int64_t tile, const CUtensorMap* amap,
+                                              const __nv_bfloat16* G, const TcGeom& g, float* y,
+                                              int64_t ld_y, const CUtensorMap* maps,
+                                              const TcSig* sigs, const TcTile* tiles) {
+    TileView v;
+    if (RAGGED) {
+        const TcTile tt = tiles[tile];
+        const TcSig sg = sigs[tt.sig];
+        v.map = maps + tt.sig;
+        v.G = G + sg.g_off;
+        v.LG = sg.LG;
+        v.k = sg.k;
+        v.m = sg.m;
+        v.nchunks = sg.nchunks;
+        v.pg = tt.pg;
+        v.vec_store = sg.vec_store & g.vec_store;  // the signal's offset and the buffer
+        v.xc0 = sg.x0 + tt.blk * kNCOL;
+        v.row0 = tt.row0;
+        v.rows = sg.rows - tt.row0;
+        v.ld = sg.seg;
+        v.y = y + sg.y_off + (int64_t)tt.row0 * sg.seg;
+        v.o0 = (int64_t)tt.blk * kNCOL + kPhT * tt.pg;
+        v.lim0 = sg.n_out - (int64_t)tt.row0 * sg.seg;
+        v.dlim = sg.seg;
+    } else {
+        const int pg = (int)(tile % kGroups);
+        const int64_t w = tile / kGroups;
+        const int64_t cg = w / g.blocks_per_cg, blk = w % g.blocks_per_cg;
+        v.map = amap;
+        v.G = G;
+        v.LG = g.LG;
+        v.k = g.k;
+        v.m = g.m;
+        v.nchunks = g.nchunks;
+        v.pg = pg;
+        v.vec_store = g.vec_store;
+        v.xc0 = (int32_t)(g.xa0 + blk * kNCOL);
+        v.row0 = (int32_t)(cg * kM);
+        v.rows = g.batch - cg * kM;
+        v.ld = ld_y;
+        v.y = y + cg * kM * ld_y;
+        v.o0 = blk * kNCOL + kPhT * pg;
+        v.lim0 = g.n_out;
+        v.dlim = 0;
+    }
+    return v;
+}
+
+template <int T, bool RAGGED>  // T bf16 terms per operand: 2 (BF16X3) or 3 (BF16X6)
 __global__ void __launch_bounds__(kThreads, 1)
 fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __restrict__ G,
-              const TcGeom g, float* __restrict__ y, int64_t ld_y, unsigned* __restrict__ err) {
+              const TcGeom g, float* __restrict__ y, int64_t ld_y, unsigned* __restrict__ err,
+              const CUtensorMap* __restrict__ maps, const TcSig* __restrict__ sigs,
+              const TcTile* __restrict__ tiles) {
     constexpr int NPROD = T == 2 ? 3 : 6;
     constexpr uint32_t kABytes = T * kABytesTerm;
     extern __shared__ uint8_t smem_raw[];
@@ -221,15 +290,12 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
     if (warp == 0) {
         // ------------------------------------------------ TMA producer
         if (lane == 0) {
-            prefetch_tmap(&amap);
+            if (!RAGGED) prefetch_tmap(&amap);
             uint32_t it = 0;
             bool ok = true;
             for (int64_t tile = blockIdx.x; ok && tile < g.n_tiles; tile += gridDim.x) {
-                const int pg = (int)(tile % kGroups);
-                const int64_t w = tile / kGroups;
-                const int64_t cg = w / g.blocks_per_cg, blk = w % g.blocks_per_cg;
-                const int64_t xc0 = g.xa0 + blk * kNCOL;
-                for (int c = 0; c < g.nchunks; ++c, ++it) {
+                const TileView v = tile_view<RAGGED>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles);
+                for (int c = 0; c < v.nchunks; ++c, ++it) {
                     const int st = (int)(it % (uint32_t)g.nstage);
                     const uint32_t ph = (it / (uint32_t)g.nstage) & 1u;
                     if (!mbar_wait(&empty[st], ph ^ 1u)) {
@@ -241,16 +307,16 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
                     mbar_arrive_expect_tx(&full[st], g.tx_bytes);
 #pragma unroll
                     for (int t = 0; t < T; ++t)
-                        tma_load_3d(sb + t * kABytesTerm, &amap, &full[st],
-                                    (int32_t)(xc0 + (int64_t)c * kKC), (int32_t)(cg * kM), t);
+                        tma_load_3d(sb + t * kABytesTerm, v.map, &full[st], v.xc0 + c * kKC,
+                                    v.row0, t);
                     uint8_t* bb = sb + kABytes;
 #pragma unroll
                     for (int t = 0; t < T; ++t)
 #pragma unroll
                         for (int l = 0; l < kPhT; ++l)
                             bulk_load(bb + (t * kPhT + l) * kBBytesPh,
-                                      G + ((int64_t)(t * kPh + kPhT * pg + l) * g.LG +
-                                           (int64_t)c * kKC),
+                                      v.G + ((int64_t)(t * kPh + kPhT * v.pg + l) * v.LG +
+                                             (int64_t)c * kKC),
                                       kBBytesPh, &full[st]);
                 }
             }
@@ -267,14 +333,14 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
             uint32_t it = 0, tcount = 0;
             bool ok = true;
             for (int64_t tile = blockIdx.x; ok && tile < g.n_tiles; tile += gridDim.x, ++tcount) {
-                const int pg = (int)(tile % kGroups);
+                const TileView v = tile_view<RAGGED>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles);
                 // the epilogue has read (and zeroed) the accumulators of the tile before
                 if (!mbar_wait(tempty, tcount & 1u)) {
                     atomicOr(err, kErrMbarTimeout);
                     break;
                 }
                 tc_fence_after();
-                for (int c = 0; c < g.nchunks; ++c, ++it) {
+                for (int c = 0; c < v.nchunks; ++c, ++it) {
                     const int st = (int)(it % (uint32_t)g.nstage);
                     const uint32_t ph = (it / (uint32_t)g.nstage) & 1u;
                     if (!mbar_wait(&full[st], ph)) {
@@ -292,7 +358,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
 #pragma unroll
                         for (int l = 0; l < kPhT; ++l) {
                             int lo, hi;
-                            live_rows(J0, 8 * (kU - 1) + kPhT * pg + l + g.m, g.k, lo, hi);
+                            live_rows(J0, 8 * (kU - 1) + kPhT * v.pg + l + v.m, v.k, lo, hi);
                             if (hi <= lo) continue;
                             const uint32_t idesc = idesc0 | ((uint32_t)((hi - lo) >> 3) << 17);
 #pragma unroll
@@ -337,17 +403,16 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
         mbar_arrive(tempty);
         uint32_t tcount = 0;
         for (int64_t tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++tcount) {
+            const TileView v = tile_view<RAGGED>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles);
             if (!mbar_wait(tfull, tcount & 1u)) {
                 if (lane == 0) atomicOr(err, kErrMbarTimeout);
                 break;
             }
             tc_fence_after();
-            const int pg = (int)(tile % kGroups);
-            const int64_t w = tile / kGroups;
-            const int64_t cg = w / g.blocks_per_cg, blk = w % g.blocks_per_cg;
-            const int64_t row = cg * kM + q * 32 + lane;
-            const int64_t o0 = blk * kNCOL + kPhT * pg;
-            float* __restrict__ yr = y + row * ld_y;
+            const int r = q * 32 + lane;  // row of the box
+            const int64_t o0 = v.o0;
+            const int64_t lim = v.lim0 - (int64_t)r * v.dlim;  // outputs of this row below lim
+            float* __restrict__ yr = v.y + (int64_t)r * v.ld;
             // every column of this warp into registers (the two accumulators
             // summed), TMEM zeroed and handed back, then the global stores:
             // the next tile's MMAs run while this tile's outputs are written
@@ -372,12 +437,12 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
             tmem_wait_st();
             tc_fence_before();
             mbar_arrive(tempty);
-            if (row < g.batch) {
+            if (r < v.rows) {
 #pragma unroll
                 for (int gi = 0; gi < kGrp; ++gi) {
                     // column u0 + i holds output ob - 8i (and the next one)
                     const int64_t ob = o0 + 8 * (kU - 1 - (c0 + 16 * gi));
-                    if (g.vec_store && ob + kPhT <= g.n_out) {
+                    if (v.vec_store && ob + kPhT <= lim) {
 #pragma unroll
                         for (int i = 0; i < 16; ++i)
                             *reinterpret_cast<float2*>(yr + ob - 8 * i) =
@@ -388,7 +453,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
 #pragma unroll
                             for (int l = 0; l < kPhT; ++l) {
                                 const int64_t o = ob - 8 * i + l;
-                                if (o < g.n_out) yr[o] = out[gi][l][i];
+                                if (o < lim) yr[o] = out[gi][l][i];
                             }
                     }
                 }
@@ -464,7 +529,7 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
             rc = set_error(SCIR_ERR_CUDA, "split kernels: %s", cudaGetErrorString(le));
     }
     if (rc == SCIR_OK) {
-        auto kern = fir_tc_kernel<T>;
+        auto kern = fir_tc_kernel<T, false>;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) {
@@ -473,7 +538,8 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
                            cudaGetErrorString(e));
         } else {
             const int64_t grid = std::min<int64_t>(g.n_tiles, (int64_t)info->sm_count);
-            kern<<<(unsigned)grid, kThreads, smem, st>>>(amap, Gs, g, a.y, a.ld_y, err);
+            kern<<<(unsigned)grid, kThreads, smem, st>>>(amap, Gs, g, a.y, a.ld_y, err, nullptr,
+                                                         nullptr, nullptr);
             cudaError_t le = cudaGetLastError();
             if (le != cudaSuccess)
                 rc = set_error(SCIR_ERR_CUDA, "launch of fir_tc_kernel failed: %s",
@@ -485,10 +551,257 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
     return rc;
 }
 
+// Per-signal split parameters of a ragged plan's tensor-core bucket.
+struct TcSplit {
+    int64_t x_off, n, plane_off, region, pad_front;  // plane elements [plane_off, +region)
+    int64_t taps_off, k, LG, g_off;
+    int32_t reverse, m;
+};
+
+// Signal i's planes: element pad_front + j holds term t of x_i[j], zero
+// elsewhere in its region (the history before the signal and the tail).
+__global__ void split_planes_ragged_kernel(const TcSplit* __restrict__ sp, const float* __restrict__ x,
+                                           int64_t plane_len, int terms,
+                                           __nv_bfloat16* __restrict__ planes) {
+    const TcSplit d = sp[blockIdx.y];
+    const float* __restrict__ xs = x + d.x_off;
+    for (int64_t e0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4; e0 < d.region;
+         e0 += (int64_t)gridDim.x * blockDim.x * 4) {
+        float v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t src = e0 + j - d.pad_front;
+            v[j] = (src >= 0 && src < d.n) ? __ldg(xs + src) : 0.0f;
+        }
+        uint2 t3[3];
+        split4_any(make_float4(v[0], v[1], v[2], v[3]), terms, t3);
+#pragma unroll
+        for (int t = 0; t < 3; ++t)
+            if (t < terms)
+                *reinterpret_cast<uint2*>(planes + t * plane_len + d.plane_off + e0) = t3[t];
+    }
+}
+
+// Signal i's tap planes G_i[t][phi][e] = term t of c[e - 8*(U-1) - phi - m].
+__global__ void split_taps_ragged_kernel(const TcSplit* __restrict__ sp, const float* __restrict__ taps,
+                                         int terms, __nv_bfloat16* __restrict__ G) {
+    const TcSplit d = sp[blockIdx.y];
+    const int64_t total = (int64_t)kPh * d.LG;
+    __nv_bfloat16* Gi = G + d.g_off;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int ph = (int)(e / d.LG);
+        const int64_t i = e % d.LG;
+        const int64_t ci = i - 8 * (int64_t)(kU - 1) - ph - d.m;
+        const float v = (ci >= 0 && ci < d.k)
+                            ? __ldg(taps + d.taps_off + (d.reverse ? d.k - 1 - ci : ci))
+                            : 0.0f;
+        const __nv_bfloat16 h1 = __float2bfloat16_rn(v);
+        const float r1 = v - __bfloat162float(h1);
+        const __nv_bfloat16 h2 = __float2bfloat16_rn(r1);
+        Gi[e] = h1;
+        Gi[total + e] = h2;
+        if (terms == 3) Gi[2 * total + e] = __float2bfloat16_rn(r1 - __bfloat162float(h2));
+    }
+}
+
+// Stage sizes of the tensor-core kernel for `terms` bf16 terms.
+int tc_stages(int terms, const DeviceInfo* info, TcGeom* g, size_t* smem) {
+    const uint32_t stage = terms * kABytesTerm + terms * kPhT * kBBytesPh;
+    g->stage_bytes = (stage + 1023) / 1024 * 1024;
+    g->tx_bytes = stage;
+    const size_t extra = 1024 + 8 * (2 * 8 + 3) + 16;
+    const int nstage =
+        (int)std::min<int64_t>(8, (info->max_smem_optin - (int64_t)extra) / g->stage_bytes);
+    if (nstage < 2) return set_error(SCIR_ERR_UNSUPPORTED, "tensor-core FIR stage too large");
+    g->nstage = nstage;
+    *smem = (size_t)nstage * g->stage_bytes + extra;
+    return SCIR_OK;
+}
+
 }  // namespace
 
 bool fir_tc_supported(const FirArgs& a) {
     return a.k >= 1 && a.n >= 1 && a.batch >= 1 && a.n_out >= 1 && a.n < (1LL << 30);
+}
+
+// ------------------------------------------------------------------ ragged bucket
+
+struct TcRaggedPlan {
+    int terms = 3;
+    int64_t nsig = 0, ntiles = 0, plane_len = 0, g_len = 0;
+    __nv_bfloat16* planes = nullptr;
+    __nv_bfloat16* G = nullptr;
+    CUtensorMap* maps = nullptr;
+    TcSig* sigs = nullptr;
+    TcTile* tiles = nullptr;
+    TcSplit* split = nullptr;
+    int64_t max_region = 0, max_g = 0;
+};
+
+void tc_ragged_destroy(TcRaggedPlan* p) {
+    if (!p) return;
+    cudaFree(p->planes);
+    cudaFree(p->G);
+    cudaFree(p->maps);
+    cudaFree(p->sigs);
+    cudaFree(p->tiles);
+    cudaFree(p->split);
+    delete p;
+}
+
+int64_t tc_ragged_tiles(const TcRaggedPlan* p) { return p ? p->ntiles : 0; }
+
+int tc_ragged_create(const TcSigIn* in, int64_t count, int terms, TcRaggedPlan** out) {
+    *out = nullptr;
+    if (count == 0) return SCIR_OK;
+    auto p = new TcRaggedPlan();
+    p->terms = terms;
+    p->nsig = count;
+    std::vector<TcSig> sig((size_t)count);
+    std::vector<TcSplit> sp((size_t)count);
+    std::vector<TcTile> tiles;
+    std::vector<int> cost;
+    int64_t plane_off = 0, g_off = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        const TcSigIn& d = in[i];
+        TcSig& S = sig[(size_t)i];
+        TcSplit& P = sp[(size_t)i];
+        const int m = (int)(((d.s % 8) + 8) % 8);
+        const int64_t xa0 = d.s - m;
+        const int64_t ktot = d.k + kNCOL - 1 + m;
+        const int nchunks = (int)ceil_div(ktot, kKC);
+        const int64_t LG = (int64_t)nchunks * kKC + 8 * kU;
+        // windows per segment row: enough that the signal needs <= 128 rows
+        const int64_t wpr = std::max<int64_t>(1, ceil_div(d.n_out, (int64_t)kM * kNCOL));
+        const int64_t seg = wpr * kNCOL;
+        const int64_t rows = ceil_div(d.n_out, seg);
+        const int64_t pad_front = (std::max<int64_t>(0, -xa0) + 7) / 8 * 8;
+        const int64_t x0 = pad_front + xa0;
+        const int64_t X = x0 + (wpr - 1) * kNCOL + (int64_t)nchunks * kKC;  // row extent
+        const int64_t region =
+            std::max((rows - 1) * seg + X, pad_front + d.n) / 8 * 8 + 8;
+        if (X >= (1LL << 31) || seg * 2 >= (1LL << 40)) {
+            tc_ragged_destroy(p);
+            return set_error(SCIR_ERR_UNSUPPORTED, "ragged tensor-core signal %lld too long",
+                             (long long)i);
+        }
+        S.g_off = g_off;
+        S.LG = LG;
+        S.k = d.k;
+        S.seg = seg;
+        S.n_out = d.n_out;
+        S.y_off = d.y_off;
+        S.m = m;
+        S.nchunks = nchunks;
+        S.x0 = (int32_t)x0;
+        S.rows = (int32_t)rows;
+        S.vec_store = (d.y_off % 2 == 0) ? 1 : 0;
+        S.pad_ = 0;
+        P.x_off = d.x_off;
+        P.n = d.n;
+        P.plane_off = plane_off;
+        P.region = region;
+        P.pad_front = pad_front;
+        P.taps_off = d.taps_off;
+        P.k = d.k;
+        P.LG = LG;
+        P.g_off = g_off;
+        P.reverse = d.reverse;
+        P.m = m;
+        plane_off += region;
+        g_off += (int64_t)terms * kPh * LG;
+        p->max_region = std::max(p->max_region, region);
+        p->max_g = std::max(p->max_g, (int64_t)kPh * LG);
+        for (int64_t blk = 0; blk < wpr; ++blk)
+            for (int pg = 0; pg < kGroups; ++pg) {
+                tiles.push_back(TcTile{(int32_t)i, 0, (int32_t)blk, pg});
+                cost.push_back(nchunks);
+            }
+    }
+    p->plane_len = (plane_off + 7) / 8 * 8;
+    p->g_len = g_off;
+    // costliest tiles first: the CTAs take tiles round-robin
+    std::vector<size_t> order(tiles.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return cost[a] > cost[b]; });
+    std::vector<TcTile> sorted(tiles.size());
+    for (size_t i = 0; i < order.size(); ++i) sorted[i] = tiles[order[i]];
+    p->ntiles = (int64_t)sorted.size();
+    auto fail = [&](int code) {
+        tc_ragged_destroy(p);
+        return code;
+    };
+    cudaError_t e = cudaMalloc(&p->planes, sizeof(__nv_bfloat16) * (size_t)terms * (size_t)p->plane_len);
+    if (e == cudaSuccess) e = cudaMalloc(&p->G, sizeof(__nv_bfloat16) * (size_t)p->g_len);
+    if (e == cudaSuccess) e = cudaMalloc(&p->maps, sizeof(CUtensorMap) * (size_t)count);
+    if (e == cudaSuccess) e = cudaMalloc(&p->sigs, sizeof(TcSig) * (size_t)count);
+    if (e == cudaSuccess) e = cudaMalloc(&p->tiles, sizeof(TcTile) * sorted.size());
+    if (e == cudaSuccess) e = cudaMalloc(&p->split, sizeof(TcSplit) * (size_t)count);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error(SCIR_ERR_OOM, "ragged tensor-core plan allocation failed: %s", cudaGetErrorString(e));
+        return fail(SCIR_ERR_OOM);
+    }
+    std::vector<CUtensorMap> maps((size_t)count);
+    for (int64_t i = 0; i < count; ++i) {
+        const TcSig& S = sig[(size_t)i];
+        const TcSplit& P = sp[(size_t)i];
+        const int64_t X = (int64_t)S.x0 + (S.seg / kNCOL - 1) * kNCOL + (int64_t)S.nchunks * kKC;
+        const int rc = make_tmap_3d(&maps[(size_t)i], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                                    p->planes + P.plane_off, (uint64_t)X, (uint64_t)S.rows,
+                                    (uint64_t)terms, (uint64_t)S.seg * 2,
+                                    (uint64_t)p->plane_len * 2, kKC, kM, 1,
+                                    CU_TENSOR_MAP_SWIZZLE_128B);
+        if (rc) return fail(rc);
+    }
+    int rc = upload_sync(p->maps, maps.data(), sizeof(CUtensorMap) * maps.size());
+    if (!rc) rc = upload_sync(p->sigs, sig.data(), sizeof(TcSig) * sig.size());
+    if (!rc) rc = upload_sync(p->tiles, sorted.data(), sizeof(TcTile) * sorted.size());
+    if (!rc) rc = upload_sync(p->split, sp.data(), sizeof(TcSplit) * sp.size());
+    if (rc) return fail(rc);
+    *out = p;
+    return SCIR_OK;
+}
+
+template <int T>
+int tc_ragged_launch(const TcRaggedPlan* p, float* y, const DeviceInfo* info, unsigned* err,
+                     cudaStream_t st) {
+    TcGeom g{};
+    size_t smem = 0;
+    int rc = tc_stages(T, info, &g, &smem);
+    if (rc) return rc;
+    g.n_tiles = p->ntiles;
+    g.vec_store = (reinterpret_cast<uintptr_t>(y) & 7) == 0 ? 1 : 0;
+    auto kern = fir_tc_kernel<T, true>;
+    SCIR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CUtensorMap unused;
+    memset(&unused, 0, sizeof(unused));
+    const int64_t grid = std::min<int64_t>(p->ntiles, (int64_t)info->sm_count);
+    kern<<<(unsigned)grid, kThreads, smem, st>>>(unused, p->G, g, y, 0, err, p->maps, p->sigs,
+                                                 p->tiles);
+    SCIR_LAUNCH_CHECK("fir_tc_kernel (ragged)");
+    return SCIR_OK;
+}
+
+int tc_ragged_run(const TcRaggedPlan* p, const float* x, const float* taps, float* y,
+                  cudaStream_t st) {
+    if (!p || p->ntiles == 0) return SCIR_OK;
+    const DeviceInfo* info = nullptr;
+    int rc = current_device(&info);
+    if (rc) return rc;
+    unsigned* err = device_error_word();
+    if (!err) return set_error(SCIR_ERR_CUDA, "device error word unavailable");
+    SCIR_REQUIRE(p->nsig <= 65535, SCIR_ERR_UNSUPPORTED, "more than 65,535 tensor-core signals");
+    const unsigned bx = (unsigned)std::min<int64_t>(ceil_div(p->max_region / 4, 256), 256);
+    split_planes_ragged_kernel<<<dim3(bx, (unsigned)p->nsig), 256, 0, st>>>(
+        p->split, x, p->plane_len, p->terms, p->planes);
+    const unsigned bt = (unsigned)std::min<int64_t>(ceil_div(p->max_g, 256), 64);
+    split_taps_ragged_kernel<<<dim3(bt, (unsigned)p->nsig), 256, 0, st>>>(p->split, taps, p->terms,
+                                                                           p->G);
+    SCIR_LAUNCH_CHECK("ragged split kernels");
+    return p->terms == 2 ? tc_ragged_launch<2>(p, y, info, err, st)
+                         : tc_ragged_launch<3>(p, y, info, err, st);
 }
 
 int launch_fir_tc(const FirArgs& a, int terms, cudaStream_t st) {

@@ -28,6 +28,33 @@ int launch_fir_simt(const FirArgs& a, bool exact, cudaStream_t st, int v = 0);
 int launch_fir_tc(const FirArgs& a, int terms, cudaStream_t st);
 bool fir_tc_supported(const FirArgs& a);
 
+// Tensor-core bucket of a ragged plan (fir_tc.cu).  Each signal is tiled as
+// up to 128 segment rows (row r = outputs [r * seg, (r + 1) * seg), seg a
+// multiple of 1,024) over one bf16 plane per term that holds the signal
+// after a zero pad of its filter history; a TMA map per signal reads the
+// rows with stride seg (overlapping).  Tiles are (signal, window of a row,
+// phase group).
+struct TcSig {
+    int64_t g_off;     // first element of the signal's tap planes [terms][8][LG]
+    int64_t LG, k;
+    int64_t seg;       // outputs per segment row
+    int64_t n_out, y_off;
+    int32_t m, nchunks, x0, rows, vec_store, pad_;
+};
+struct TcTile {
+    int32_t sig, row0, blk, pg;
+};
+struct TcSigIn {       // one signal as the ragged plan describes it
+    int64_t x_off, n, taps_off, k, y_off, s, n_out;
+    int reverse;
+};
+struct TcRaggedPlan;
+int tc_ragged_create(const TcSigIn* sigs, int64_t count, int terms, TcRaggedPlan** out);
+void tc_ragged_destroy(TcRaggedPlan* p);
+int64_t tc_ragged_tiles(const TcRaggedPlan* p);
+int tc_ragged_run(const TcRaggedPlan* p, const float* x, const float* taps, float* y,
+                  cudaStream_t st);
+
 // Polyphase FIR: y[m] = sum_q h[ph + q*up] * x[base - q],
 // t = m*down + off, ph = t mod up, base = t div up, m in [0, n_out).
 struct PolyArgs {

@@ -30,6 +30,11 @@ struct RaggedTile {
 
 struct scir_ragged_plan {
     int device = -1, mode = 0, precision = 0;
+    // tensor-core bucket: signals with at least tc_min_taps taps (AUTO, BF16X3,
+    // BF16X6) run the split-bf16 tensor-core contraction in its own launch
+    int tc_terms = 0, tc_min_taps = 1 << 30;
+    std::vector<char> in_tc;          // per signal
+    scir::TcRaggedPlan* tc = nullptr;
     int64_t count = 0, ntiles = 0, samples_in = 0;
     double macs = 0.0;
     RaggedSig* d_sigs = nullptr;
@@ -88,6 +93,7 @@ int build_tiles(scir_ragged_plan* p, int v16_min_taps) {
     std::vector<double> cost;
     for (size_t i = 0; i < p->h_sigs.size(); ++i) {
         const RaggedSig& s = p->h_sigs[i];
+        if (!p->in_tc.empty() && p->in_tc[i]) continue;  // served by the tensor-core bucket
         const int v16 = s.k >= v16_min_taps ? 1 : 0;
         const int64_t tile = (int64_t)kFirThreads * (v16 ? 16 : 8);
         for (int64_t o0 = 0; o0 < s.n_out; o0 += tile) {
@@ -125,6 +131,27 @@ int build_tiles(scir_ragged_plan* p, int v16_min_taps) {
     return SCIR_OK;
 }
 
+// Rebuilds the tensor-core bucket with the signals that have at least
+// min_taps taps and 16,384 outputs (fewer outputs leave most of a 128-row
+// tile empty), then the CUDA-core tile list for the others.
+int build_tc(scir_ragged_plan* p, int min_taps) {
+    tc_ragged_destroy(p->tc);
+    p->tc = nullptr;
+    p->in_tc.assign(p->h_sigs.size(), 0);
+    p->tc_min_taps = min_taps;
+    if (p->tc_terms == 0) return build_tiles(p, p->v16_min_taps);
+    std::vector<TcSigIn> in;
+    for (size_t i = 0; i < p->h_sigs.size(); ++i) {
+        const RaggedSig& s = p->h_sigs[i];
+        if (s.k < min_taps || s.n_out < 16384) continue;
+        p->in_tc[i] = 1;
+        in.push_back(TcSigIn{s.x_off, s.n, s.taps_off, s.k, s.y_off, s.s, s.n_out, s.reverse});
+    }
+    int rc = tc_ragged_create(in.data(), (int64_t)in.size(), p->tc_terms, &p->tc);
+    if (rc) return rc;
+    return build_tiles(p, p->v16_min_taps);
+}
+
 }  // namespace
 }  // namespace scir
 
@@ -137,9 +164,14 @@ SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count
     *plan = nullptr;
     SCIR_REQUIRE(count >= 0 && (count == 0 || desc), SCIR_ERR_INVALID_ARG, "bad descriptor table");
     SCIR_REQUIRE(count < (1LL << 31), SCIR_ERR_UNSUPPORTED, "too many signals");
-    if (precision == SCIR_PREC_AUTO) precision = SCIR_PREC_FP32;
+    // AUTO, BF16X6, BF16X3: long filters on the tensor cores (split-bf16 with
+    // three or two terms), the rest in FP32 on the CUDA cores
+    int tc_terms = 0;
+    if (precision == SCIR_PREC_AUTO || precision == SCIR_PREC_BF16X6) tc_terms = 3;
+    if (precision == SCIR_PREC_BF16X3) tc_terms = 2;
+    if (tc_terms) precision = SCIR_PREC_FP32;
     SCIR_REQUIRE(precision == SCIR_PREC_FP32 || precision == SCIR_PREC_REF_EXACT,
-                 SCIR_ERR_UNSUPPORTED, "ragged launch serves FP32 and REF_EXACT precision");
+                 SCIR_ERR_UNSUPPORTED, "unknown ragged precision");
     const DeviceInfo* info = nullptr;
     int rc = current_device(&info);
     if (rc) return rc;
@@ -148,6 +180,7 @@ SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count
     p->device = info->device;
     p->mode = mode;
     p->precision = precision;
+    p->tc_terms = tc_terms;
     p->count = count;
     std::vector<RaggedSig> sigs((size_t)count);
     for (int64_t i = 0; i < count; ++i) {
@@ -203,7 +236,7 @@ SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count
         return fail(SCIR_ERR_CUDA);
     }
     p->per_sm = per_sm;
-    rc = build_tiles(p, p->v16_min_taps);
+    rc = build_tc(p, tc_terms ? 512 : (1 << 30));
     if (rc) return fail(rc);
     *plan = p;
     return SCIR_OK;
@@ -214,6 +247,7 @@ SCIR_API int scir_ragged_plan_destroy(scir_ragged_plan* plan) {
     if (plan->d_sigs) cudaFree(plan->d_sigs);
     if (plan->d_tiles) cudaFree(plan->d_tiles);
     if (plan->d_counter) cudaFree(plan->d_counter);
+    scir::tc_ragged_destroy(plan->tc);
     delete plan;
     return SCIR_OK;
 }
@@ -221,7 +255,7 @@ SCIR_API int scir_ragged_plan_destroy(scir_ragged_plan* plan) {
 SCIR_API int scir_ragged_plan_stats(const scir_ragged_plan* plan, int64_t* tiles, double* macs,
                                     int64_t* samples_in) {
     SCIR_REQUIRE(plan != nullptr, SCIR_ERR_INVALID_ARG, "plan is NULL");
-    if (tiles) *tiles = plan->ntiles;
+    if (tiles) *tiles = plan->ntiles + scir::tc_ragged_tiles(plan->tc);
     if (macs) *macs = plan->macs;
     if (samples_in) *samples_in = plan->samples_in;
     return SCIR_OK;
@@ -231,13 +265,17 @@ SCIR_API int scir_fir_ragged_f32(const scir_ragged_plan* plan, const float* x, c
                                  float* y, void* stream) {
     clear_error();
     SCIR_REQUIRE(plan != nullptr, SCIR_ERR_INVALID_ARG, "plan is NULL");
-    if (plan->ntiles == 0) return SCIR_OK;
+    if (plan->ntiles == 0 && !plan->tc) return SCIR_OK;
     SCIR_REQUIRE(x && taps && y, SCIR_ERR_INVALID_ARG, "NULL buffer");
     int dev = -1;
     SCIR_CUDA_TRY(cudaGetDevice(&dev));
     SCIR_REQUIRE(dev == plan->device, SCIR_ERR_INVALID_ARG,
                  "plan was built on device %d, current device is %d", plan->device, dev);
     cudaStream_t st = as_stream(stream);
+    // the tensor-core bucket first (split kernels + one persistent launch)
+    int rc = scir::tc_ragged_run(plan->tc, x, taps, y, st);
+    if (rc) return rc;
+    if (plan->ntiles == 0) return SCIR_OK;
     SCIR_CUDA_TRY(cudaMemsetAsync(plan->d_counter, 0, sizeof(unsigned long long), st));
     if (plan->precision == SCIR_PREC_REF_EXACT)
         ragged_kernel<true><<<plan->grid, kFirThreads, plan->smem, st>>>(
@@ -254,46 +292,77 @@ SCIR_API int scir_ragged_plan_autotune(scir_ragged_plan* plan, const float* x, c
                                        double* best_ms) {
     clear_error();
     SCIR_REQUIRE(plan != nullptr, SCIR_ERR_INVALID_ARG, "plan is NULL");
-    if (plan->ntiles == 0) return SCIR_OK;
+    if (plan->ntiles == 0 && !plan->tc) return SCIR_OK;
     SCIR_REQUIRE(x && taps && y, SCIR_ERR_INVALID_ARG, "NULL buffer");
     cudaStream_t st = as_stream(stream);
-    // the tile list is rebuilt: nothing queued on the stream may still read it
+    // the tile lists are rebuilt: nothing queued on the stream may still read them
     SCIR_CUDA_TRY(cudaStreamSynchronize(st));
-    static const int kCand[] = {32, 64, 128, 256, 512, 1 << 30};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     SCIR_CUDA_TRY(cudaEventCreate(&e0));
     SCIR_CUDA_TRY(cudaEventCreate(&e1));
+    auto time_plan = [&](float* ms) -> int {
+        int rc = scir_fir_ragged_f32(plan, x, taps, y, stream);  // warm-up
+        if (rc) return rc;
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < 2 && rc == SCIR_OK; ++r) rc = scir_fir_ragged_f32(plan, x, taps, y, stream);
+        cudaEventRecord(e1, st);
+        if (rc) return rc;
+        cudaError_t ce = cudaEventSynchronize(e1);
+        if (ce == cudaSuccess) ce = cudaEventElapsedTime(ms, e0, e1);
+        if (ce != cudaSuccess)
+            return set_error(SCIR_ERR_CUDA, "ragged autotune timing: %s", cudaGetErrorString(ce));
+        *ms *= 0.5f;
+        return SCIR_OK;
+    };
+    // 1. the tap count from which CUDA-core tiles use 16 outputs per thread
+    static const int kCand[] = {32, 64, 128, 256, 512, 1 << 30};
     int best = plan->v16_min_taps, rc = SCIR_OK;
     float best_t = 0.0f;
     for (int c : kCand) {
         rc = build_tiles(plan, c);
-        if (rc) break;
-        rc = scir_fir_ragged_f32(plan, x, taps, y, stream);  // warm-up
-        if (rc) break;
-        cudaEventRecord(e0, st);
-        for (int r = 0; r < 2 && rc == SCIR_OK; ++r) rc = scir_fir_ragged_f32(plan, x, taps, y, stream);
-        cudaEventRecord(e1, st);
-        if (rc) break;
-        cudaError_t ce = cudaEventSynchronize(e1);
         float ms = 0.0f;
-        if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
-        if (ce != cudaSuccess) {
-            rc = set_error(SCIR_ERR_CUDA, "ragged autotune timing: %s", cudaGetErrorString(ce));
-            break;
-        }
-        ms *= 0.5f;
+        if (!rc) rc = time_plan(&ms);
+        if (rc) break;
         if (best_t == 0.0f || ms < best_t) {
             best_t = ms;
             best = c;
         }
     }
+    if (!rc) rc = build_tiles(plan, best);
+    // 2. the tap count from which signals go to the tensor cores
+    if (!rc && plan->tc_terms) {
+        static const int kTc[] = {256, 512, 1024, 2048, 1 << 30};
+        int best_tc = plan->tc_min_taps;
+        float best_tc_t = 0.0f;
+        for (int c : kTc) {
+            rc = build_tc(plan, c);
+            float ms = 0.0f;
+            if (!rc) rc = time_plan(&ms);
+            if (rc) break;
+            if (best_tc_t == 0.0f || ms < best_tc_t) {
+                best_tc_t = ms;
+                best_tc = c;
+            }
+        }
+        if (!rc) rc = build_tc(plan, best_tc);
+        if (!rc) best_t = best_tc_t;
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
-    rc = build_tiles(plan, best);
-    if (rc) return rc;
     if (v16_min_taps) *v16_min_taps = best;
     if (best_ms) *best_ms = best_t;
+    return SCIR_OK;
+}
+
+SCIR_API int scir_ragged_plan_tensor_cores(const scir_ragged_plan* plan, int* min_taps,
+                                           int64_t* signals) {
+    clear_error();
+    SCIR_REQUIRE(plan != nullptr, SCIR_ERR_INVALID_ARG, "plan is NULL");
+    int64_t cnt = 0;
+    for (char c : plan->in_tc) cnt += c ? 1 : 0;
+    if (min_taps) *min_taps = plan->tc_terms ? plan->tc_min_taps : 0;
+    if (signals) *signals = cnt;
     return SCIR_OK;
 }
 

@@ -100,3 +100,73 @@ def test_library_graph_capture_mixed_calls(cuda):
         assert torch.equal(a, b)
     g.close()
     plan.close()
+
+
+# ------------------------------------------ tensor-core bucket (AUTO, BF16X6 / BF16X3)
+# Signals with >= 512 taps and >= 16,384 outputs run the split-bf16
+# contraction as segment rows (up to 128 per signal) in their own persistent
+# launch; the rest stay on the CUDA cores.  Both buckets are checked against
+# the FP64 oracle, with odd output offsets (scalar stores) among them.
+def _mixed_set(seed, count):
+    rng = np.random.default_rng(seed)
+    n = np.exp(rng.uniform(np.log(1000), np.log(400000), count)).round().astype(np.int64)
+    k = np.exp(rng.uniform(np.log(16), np.log(2048), count)).round().astype(np.int64)
+    n[:3] = [300000, 20000, 150001]
+    k[:3] = [2048, 600, 4095]
+    x = rng.uniform(-1, 1, int(n.sum())).astype(np.float32)
+    taps = (rng.standard_normal(int(k.sum())) / np.sqrt(np.repeat(k, k))).astype(np.float32)
+    return n, k, x, taps
+
+
+@pytest.mark.parametrize("prec,tol", [(S.Precision.AUTO, 1e-5), (S.Precision.BF16X3, 3e-5)])
+@pytest.mark.parametrize("mode", [S.FirMode.LFILTER, S.FirMode.REF_CORR, S.FirMode.FULL,
+                                  S.FirMode.VALID])
+def test_ragged_tensor_core_bucket(cuda, prec, tol, mode):
+    import torch
+    n, k, x, taps = _mixed_set(int(mode) + 10, 24)
+    n = np.maximum(n, k)  # VALID needs n >= k
+    x = np.random.default_rng(3).uniform(-1, 1, int(n.sum())).astype(np.float32)
+    # odd gaps between the outputs of consecutive signals
+    n_out = np.array([S.fir_out_len(int(a), int(b), mode) for a, b in zip(n, k)])
+    y_off = np.concatenate([[1], np.cumsum(n_out + 3)[:-1] + 1]).astype(np.int64)
+    plan = S.RaggedPlan(n, k, mode, prec, y_off=y_off)
+    tc_taps, tc_count = plan.tensor_cores()
+    assert tc_taps == 512 and 3 <= tc_count < len(n)
+    y = torch.full((int(y_off[-1] + n_out[-1] + 2),), float("nan"), device=cuda)
+    plan.run(torch.from_numpy(x).to(cuda), torch.from_numpy(taps).to(cuda), y)
+    y = y.cpu().numpy()
+    for i in range(len(n)):
+        xi = x[plan.x_off[i]:plan.x_off[i] + n[i]].astype(np.float64)
+        ti = taps[plan.taps_off[i]:plan.taps_off[i] + k[i]].astype(np.float64)
+        ref = O.fir_mode_f64(xi, ti, int(mode))[0]
+        yi = y[y_off[i]:y_off[i] + n_out[i]]
+        assert normwise_err(yi, ref) < tol, (i, int(n[i]), int(k[i]))
+    plan.close()
+
+
+def test_ragged_tensor_core_graph_and_autotune(cuda):
+    import torch
+    n, k, x, taps = _mixed_set(31, 16)
+    plan = S.RaggedPlan(n, k, S.FirMode.LFILTER, S.Precision.AUTO)
+    xd, td = torch.from_numpy(x).to(cuda), torch.from_numpy(taps).to(cuda)
+    y = torch.zeros(plan.y_len, device=cuda)
+    plan.autotune(xd, td, y)
+    plan.run(xd, td, y)
+    ref = y.clone()
+    y2 = torch.zeros_like(y)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            plan.run(xd, td, y2, stream=s)
+    for _ in range(2):
+        y2.fill_(float("nan"))
+        g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(ref, y2)
+    for i in range(len(n)):
+        xi = x[plan.x_off[i]:plan.x_off[i] + n[i]].astype(np.float64)
+        ti = taps[plan.taps_off[i]:plan.taps_off[i] + k[i]].astype(np.float64)
+        ref_i = O.fir_mode_f64(xi, ti, int(S.FirMode.LFILTER))[0]
+        assert normwise_err(y2[plan.y_off[i]:plan.y_off[i] + n[i]].cpu().numpy(), ref_i) < 1e-5
+    plan.close()
