@@ -593,10 +593,22 @@ class Ragged(Workload):
         self.torch.cuda.synchronize()
 
     def step(self, stream, precision=None):
-        if self.graph is not None:
+        if precision is not None and precision != self.precision:
+            self.other_plan(precision).run(self.x, self.taps, self.y, stream=stream)
+        elif self.graph is not None:
             self.graph.launch(stream)
         else:
             self.plan.run(self.x, self.taps, self.y, stream=stream)
+
+    def other_plan(self, precision):
+        """A plan of the same signals at another precision (FP32: no
+        tensor-core bucket), autotuned once on first use."""
+        plans = self.__dict__.setdefault("plans", {})
+        if precision not in plans:
+            plan = self.S.RaggedPlan(self.n, self.k, self.S.FirMode.LFILTER, precision)
+            plan.autotune(self.x, self.taps, self.y)
+            plans[precision] = plan
+        return plans[precision]
 
     def autotune(self):
         thr, ms = self.plan.autotune(self.x, self.taps, self.y)
@@ -622,7 +634,7 @@ class Ragged(Workload):
 
     def max_rel_err(self, precision=None):
         import scipy.signal as ss
-        self.step(None)
+        self.step(None, precision)
         self.torch.cuda.synchronize()
         errs = []
         for i in np.argsort(self.n)[:: max(1, len(self.n) // 6)][:6]:

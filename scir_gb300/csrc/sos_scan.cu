@@ -13,8 +13,12 @@
 //        S_0 = zi,  S_{b+1} = Phi S_b + f_b,  Phi = A^L,
 //      A the one-sample state transition of the cascade with zero input (in
 //      the DF2T coordinates the API exchanges states in), Phi formed on the
-//      host in FP64 by repeated squaring; one warp per channel runs the scan
-//      in FP64 (lane i holds state component i);
+//      host in FP64 by repeated squaring; one warp runs a scan in FP64 (lane
+//      i holds state component i).  With many blocks the scan has two
+//      levels, so its sequential depth is ~3 sqrt(nb) steps, not nb: groups
+//      of m blocks are scanned from zero state at the same time (their end
+//      states F_g), the group entry states follow from G_{g+1} = Phi^m G_g +
+//      F_g, and every group is scanned again from G_g;
 //   3. every block is filtered again from S_b, which gives the outputs of
 //      the sequential recursion; the samples past the last whole block are
 //      filtered from S_nb, and the final state goes to zf.
@@ -41,7 +45,8 @@ constexpr int kMaxScanStates = 32;  // 2 x 16 sections
 // S_{b+1} = Phi S_b + f_b for one channel per CTA (one warp, lane i holds
 // state component i; S states): f [ch][nb][S] final states of the
 // zero-state blocks, zi [ch][S] or null; writes the states entering every
-// block, sin [ch][nb][S], and the state after the last block, fin [ch][S].
+// block, sin [ch][nb][S], and the state after the last block, fin [ch][S]
+// (either output may be null).
 // The f values of the next 32 blocks are loaded together, so a step waits
 // only for the shuffles and FMAs of the recurrence itself.
 template <int S>
@@ -57,7 +62,7 @@ sos_block_scan_kernel(const double* __restrict__ phi, const double* __restrict__
     for (int j = 0; j < S; ++j) prow[j] = on ? phi[i * S + j] : 0.0;
     double s = (on && zi) ? zi[ch * S + i] : 0.0;
     const double* fc = f + ch * nb * S;
-    double* sc = sin + ch * nb * S;
+    double* sc = sin ? sin + ch * nb * S : nullptr;
     for (int64_t b0 = 0; b0 < nb; b0 += 32) {
         double fb[32];
 #pragma unroll
@@ -65,7 +70,7 @@ sos_block_scan_kernel(const double* __restrict__ phi, const double* __restrict__
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
             if (b0 + j >= nb) break;
-            if (on) sc[(b0 + j) * S + i] = s;
+            if (on && sin) sc[(b0 + j) * S + i] = s;
             double acc[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
             for (int q = 0; q < S; ++q)
@@ -73,7 +78,7 @@ sos_block_scan_kernel(const double* __restrict__ phi, const double* __restrict__
             s = (acc[0] + acc[1]) + (acc[2] + acc[3]) + fb[j];
         }
     }
-    if (on) fin[ch * S + i] = s;
+    if (on && fin) fin[ch * S + i] = s;
 }
 
 template <int S>
@@ -158,22 +163,40 @@ int64_t sos_scan_blocks(int64_t batch, int64_t n, int nsec, int precision, bool 
     return nb >= 64 ? nb : 0;
 }
 
+// Blocks per group of the two-level scan (0: one level): about sqrt(nb),
+// a power of two >= 64 that divides nb, from 256 blocks up.
+static int64_t scan_group(int64_t nb) {
+    if (nb < 256) return 0;
+    int64_t m = 64;
+    while (nb % (2 * m) == 0 && 4 * m * m <= nb) m *= 2;
+    return m;
+}
+
 template <typename T>
 int sosfilt_blocked(const T* x, int64_t ld_x, int64_t batch, int64_t n, const SosCoef& c,
                     const double* zi, double* zf, int precision, T* y, int64_t ld_y, int64_t nb,
                     cudaStream_t st) {
     const int S = 2 * c.nsec;
     const int64_t L = n / nb, tail = n - nb * L;
-    std::vector<double> phi;
+    const int64_t m = scan_group(nb), ng = m ? nb / m : 0;
+    // Phi = A^L, then (two levels) Phi^m = A^(L m), in one upload
+    std::vector<double> phi, phim;
     cascade_phi(c, L, phi);
+    if (m) {
+        cascade_phi(c, L * m, phim);
+        phi.insert(phi.end(), phim.begin(), phim.end());
+    }
     double* d_phi = nullptr;
     double* f = nullptr;
     double* sin = nullptr;
     double* fin = nullptr;
+    double* grp = nullptr;  // two levels: F_g, then G_g, [ch][ng][S] each
     int rc = scratch_alloc((void**)&d_phi, sizeof(double) * phi.size(), st);
     if (!rc) rc = scratch_alloc((void**)&f, sizeof(double) * (size_t)(batch * nb * S), st);
     if (!rc) rc = scratch_alloc((void**)&sin, sizeof(double) * (size_t)(batch * nb * S), st);
     if (!rc) rc = scratch_alloc((void**)&fin, sizeof(double) * (size_t)(batch * S), st);
+    if (!rc && m)
+        rc = scratch_alloc((void**)&grp, sizeof(double) * (size_t)(2 * batch * ng * S), st);
     if (!rc) {
         cudaError_t e = cudaMemcpyAsync(d_phi, phi.data(), sizeof(double) * phi.size(),
                                         cudaMemcpyHostToDevice, st);
@@ -183,7 +206,19 @@ int sosfilt_blocked(const T* x, int64_t ld_x, int64_t batch, int64_t n, const So
     if (!rc)
         rc = launch_sosfilt<T>(x, ld_x, batch * nb, L, c, nullptr, f, precision, y, ld_y, st, nb, L);
     // 2. the states entering every block
-    if (!rc) rc = scan_dispatch(S, d_phi, f, zi, batch, nb, sin, fin, st);
+    if (!rc && !m) rc = scan_dispatch(S, d_phi, f, zi, batch, nb, sin, fin, st);
+    if (!rc && m) {
+        double* F = grp;
+        double* G = grp + batch * ng * S;
+        const double* d_phim = d_phi + (size_t)S * S;
+        // groups of m blocks from zero state (each group a channel of the
+        // one-level scan): their end states F
+        rc = scan_dispatch(S, d_phi, f, nullptr, batch * ng, m, nullptr, F, st);
+        // the group entry states G and the state after the last group
+        if (!rc) rc = scan_dispatch(S, d_phim, F, zi, batch, ng, G, fin, st);
+        // every group again from its entry state: the states entering every block
+        if (!rc) rc = scan_dispatch(S, d_phi, f, G, batch * ng, m, sin, nullptr, st);
+    }
     // 3. every block again from its true state; the samples past the last
     //    block from the state after it; the final state
     if (!rc)
@@ -200,6 +235,7 @@ int sosfilt_blocked(const T* x, int64_t ld_x, int64_t batch, int64_t n, const So
     scratch_free(f, st);
     scratch_free(sin, st);
     scratch_free(fin, st);
+    scratch_free(grp, st);
     return rc;
 }
 template int sosfilt_blocked<float>(const float*, int64_t, int64_t, int64_t, const SosCoef&,

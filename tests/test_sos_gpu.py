@@ -231,7 +231,8 @@ def test_fp32_pipe_channel_halves(cuda, batch):
 # FP32-state modes keep their 1e-5 bound; FP64 state takes the path with
 # blocks of >= 65,536 samples and a stated bound of 1e-9; FP64_EXACT stays
 # sequential (bit-identical to the reference order).
-@pytest.mark.parametrize("batch,n", [(1, 1 << 20), (2, 3_000_017), (5, 700_001)])
+@pytest.mark.parametrize("batch,n", [(1, 1 << 20), (2, 3_000_017), (5, 700_001), (1, 1 << 24),
+                                     (3, 200_000)])
 def test_block_scan_fp32_coupled(cuda, batch, n):
     rng = np.random.default_rng(batch + n)
     x = rng.standard_normal((batch, n)).astype(np.float32)
