@@ -83,13 +83,20 @@ typedef enum scir_fir_mode {
  *   bf16 hi+lo, three products (hi*hi + hi*lo + lo*hi), FP32 accumulate.
  * SCIR_PREC_BF16X6: tensor cores, operands split into three bf16 terms,
  *   six products; FP32-level accuracy.
- * SCIR_PREC_AUTO: the library picks (autotuned, accuracy <= 1e-5 normwise). */
+ * SCIR_PREC_FP16X3: tensor cores, each signal row and the taps scaled by a
+ *   power of two (from their largest finite magnitude) and split into fp16
+ *   hi+lo (22 significant bits), three products; BF16X6's accuracy at
+ *   BF16X3's cost.  FIR entry points only (the polyphase path has no such
+ *   form: SCIR_ERR_UNSUPPORTED).
+ * SCIR_PREC_AUTO: the library picks (autotuned, accuracy <= 1e-5 normwise;
+ *   on the tensor cores the FP16X3 form). */
 typedef enum scir_precision {
     SCIR_PREC_AUTO = -1,
     SCIR_PREC_REF_EXACT = 0,
     SCIR_PREC_FP32 = 1,
     SCIR_PREC_BF16X3 = 2,
-    SCIR_PREC_BF16X6 = 3
+    SCIR_PREC_BF16X6 = 3,
+    SCIR_PREC_FP16X3 = 4
 } scir_precision;
 
 /* Arithmetic of the second-order-section recursion.
@@ -207,9 +214,9 @@ typedef struct scir_ragged_plan scir_ragged_plan;
 /* Builds a launch plan from a HOST descriptor table: validates every entry,
  * splits signals into work tiles, orders them longest-first and uploads the
  * tile table to the device.  Precision: SCIR_PREC_FP32 / REF_EXACT run every
- * signal on the CUDA cores; SCIR_PREC_AUTO (or BF16X6, BF16X3) sends the
- * signals with at least 512 taps (autotunable) and 16,384 outputs to the
- * tensor cores (split-bf16 contraction, three or two terms) in a second
+ * signal on the CUDA cores; SCIR_PREC_AUTO (or FP16X3, BF16X6, BF16X3) sends
+ * the signals with at least 512 taps (autotunable) and 16,384 outputs to the
+ * tensor cores (split-operand contraction; AUTO: FP16X3) in a second
  * persistent launch, the rest to the CUDA cores in FP32. */
 SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count,
                                      int mode, int precision,
@@ -310,8 +317,8 @@ SCIR_API int scir_graph_destroy(scir_graph* graph);
 /* ----------------------------------------------------------------------- */
 
 /* Batched FIR: CUDA-core tiles of 8 or 16 outputs per thread, and for
- * SCIR_PREC_AUTO also the tensor-core BF16X6 form.  precision must be
- * REF_EXACT, FP32 or AUTO (the split-bf16 modes have one form). */
+ * SCIR_PREC_AUTO also the tensor-core FP16X3 form.  precision must be
+ * REF_EXACT, FP32 or AUTO (the split-operand modes have one form). */
 SCIR_API int scir_autotune_fir(int64_t batch, int64_t n, int64_t k, int mode,
                                int precision, double* best_ms, char* choice,
                                size_t choice_len);

@@ -50,6 +50,7 @@ class Precision(enum.IntEnum):
     FP32 = 1       # FP32 FMA on CUDA cores ("plain")
     BF16X3 = 2     # tensor cores, bf16 hi+lo operands, 3 products
     BF16X6 = 3     # tensor cores, 3-term bf16 operands, 6 products
+    FP16X3 = 4     # tensor cores, power-of-two scaled fp16 hi+lo operands, 3 products
 
 
 class SosPrecision(enum.IntEnum):

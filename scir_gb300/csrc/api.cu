@@ -308,17 +308,20 @@ int fir_dispatch(const FirArgs& a, int precision, cudaStream_t st) {
     if (tuned == 1 || tuned == 2)
         return launch_fir_simt(a, precision == SCIR_PREC_REF_EXACT, st, tuned == 1 ? 8 : 16);
     if (tuned == 3 && precision == SCIR_PREC_AUTO && fir_tc_supported(a))
-        return launch_fir_tc(a, 3, st);
+        return launch_fir_tc(a, kTcFp16x3, st);
     switch (precision) {
     case SCIR_PREC_REF_EXACT: return launch_fir_simt(a, true, st);
     case SCIR_PREC_FP32: return launch_fir_simt(a, false, st);
     case SCIR_PREC_BF16X3:
     case SCIR_PREC_BF16X6:
+    case SCIR_PREC_FP16X3:
         if (!fir_tc_supported(a))
             return set_error(SCIR_ERR_UNSUPPORTED, "tensor-core FIR does not serve this shape");
-        return launch_fir_tc(a, precision == SCIR_PREC_BF16X3 ? 2 : 3, st);
+        return launch_fir_tc(a, precision == SCIR_PREC_BF16X3   ? kTcBf16x3
+                                : precision == SCIR_PREC_BF16X6 ? kTcBf16x6
+                                                                : kTcFp16x3, st);
     case SCIR_PREC_AUTO:
-        if (a.k >= 512 && fir_tc_supported(a)) return launch_fir_tc(a, 3, st);
+        if (a.k >= 512 && fir_tc_supported(a)) return launch_fir_tc(a, kTcFp16x3, st);
         return launch_fir_simt(a, false, st);
     default: return set_error(SCIR_ERR_INVALID_ARG, "unknown precision %d", precision);
     }
@@ -337,6 +340,8 @@ int poly_dispatch(const PolyArgs& a, int precision, cudaStream_t st) {
         if (!poly_tc_supported(a))
             return set_error(SCIR_ERR_UNSUPPORTED, "tensor-core polyphase does not serve this shape");
         return launch_poly_tc(a, precision == SCIR_PREC_BF16X3 ? 2 : 3, st);
+    case SCIR_PREC_FP16X3:
+        return set_error(SCIR_ERR_UNSUPPORTED, "FP16X3 serves the FIR entry points only");
     default: return set_error(SCIR_ERR_INVALID_ARG, "unknown precision %d", precision);
     }
 }
@@ -384,7 +389,7 @@ SCIR_API int scir_fir_batched_f32(const float* x, int64_t ld_x, int64_t batch, i
                                   int64_t ld_y, void* stream) {
     clear_error();
     SCIR_REQUIRE(k >= 0, SCIR_ERR_INVALID_ARG, "negative tap count");
-    SCIR_REQUIRE(precision >= SCIR_PREC_AUTO && precision <= SCIR_PREC_BF16X6,
+    SCIR_REQUIRE(precision >= SCIR_PREC_AUTO && precision <= SCIR_PREC_FP16X3,
                  SCIR_ERR_INVALID_ARG, "unknown precision %d", precision);
     cudaStream_t st = as_stream(stream);
     FirArgs a;

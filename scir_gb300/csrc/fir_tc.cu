@@ -1,5 +1,5 @@
 // Batched FIR on the 5th-generation tensor cores (tcgen05, kind::f16) with
-// split-bf16 operands and FP32 accumulation in TMEM, in one pass.
+// split bf16 or fp16 operands and FP32 accumulation in TMEM, in one pass.
 //
 // Contraction.  Outputs are grouped in windows of 1,024 (o0 .. o0+1023) and
 // split by output phase phi = r mod 8 (r = o - o0 = 8u + phi, u < 128).  For
@@ -19,7 +19,14 @@
 // N<=128 (outputs of one phase) x K=16.
 //
 // Precision.  x = x1 + x2 [+ x3] and c = c1 + c2 [+ c3] in bf16 terms;
-// BF16X3 forms x1c1 + (x1c2 + x2c1), BF16X6 adds x1c3 + x2c2 + x3c1.  The
+// BF16X3 forms x1c1 + (x1c2 + x2c1), BF16X6 adds x1c3 + x2c2 + x3c1.
+// FP16X3 forms the three products of BF16X3 from two fp16 terms: fp16 keeps
+// 11 significant bits to bf16's 8, so x1 + x2 holds 22 bits of x (bf16:
+// 16) and the dropped x2c2 is 2^-22 of x1c1 -- BF16X6's accuracy for
+// BF16X3's MMAs.  fp16's range is narrow, so every signal row is scaled by
+// 2^e before the split (max |x| 2^e < 2^15, from a max pass over the row's
+// finite samples) and the taps by their own 2^f; the epilogue multiplies by
+// 2^-(e+f), which is exact.  The
 // dominant x1c1 and the sum of the cross terms go to two separate FP32
 // accumulators (cross terms added into the large x1c1 sum would be rounded
 // against its magnitude; kept apart they are rounded against their own,
@@ -62,6 +69,7 @@
 #include "sm100.cuh"
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cstring>
@@ -84,6 +92,9 @@ constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr int kTmemCols = 512;
 constexpr uint32_t kABytesTerm = kM * kKC * 2;  // 16 KB
 constexpr int kCrossCol = kPhT * kU;            // first column of the cross accumulators
+
+// One operand element in the term planes: bf16 or fp16, by form.
+using op16 = uint16_t;
 
 struct TcGeom {
     int nstage, nchunks, m;
@@ -115,16 +126,91 @@ __device__ __forceinline__ void split4_any(const float4 v, int terms, uint2 (&ou
     }
 }
 
-// x -> bf16 term planes xs[t][b][i] = term t of x[b][i] (zero for
-// n <= i < nA).  Each thread converts 4 consecutive elements: the loads are
-// coalesced across the warp and each plane gets one 8-byte store.
+// ---- FP16X3 scaling.  mx holds the bit pattern of max |v| over the finite
+// values of a row (0 for none); a row is scaled by 2^f16_shift(mx) so its
+// largest magnitude is below 2^15 (fp16 holds up to 65,504).  Shifts are
+// clamped to [-100, 100], so a sum of two is undone by two exact multiplies.
+__device__ __forceinline__ int f16_shift(unsigned maxbits) {
+    if (maxbits == 0u || maxbits >= 0x7f800000u) return 0;
+    const int E = (int)(maxbits >> 23);  // biased exponent: max |v| < 2^(E - 126)
+    const int sh = 141 - (E > 0 ? E : 1);
+    return sh < -100 ? -100 : sh > 100 ? 100 : sh;
+}
+__device__ __forceinline__ float pow2f(int e) {  // 2^e, e in [-126, 127]
+    return __int_as_float((e + 127) << 23);
+}
+
+// Max |v| over the finite values of v[0, len), ORed into *out as bits (the
+// order of non-negative floats is the order of their bit patterns).
+__device__ __forceinline__ void absmax_segment(const float* __restrict__ v, int64_t len,
+                                               unsigned* out) {
+    unsigned m = 0u;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned b = __float_as_uint(__ldg(v + i)) & 0x7fffffffu;
+        if (b < 0x7f800000u && b > m) m = b;
+    }
+    m = __reduce_max_sync(0xffffffffu, m);
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+// mx[b] for every signal row b < batch, mx[batch] for the taps (mx zeroed).
+__global__ void absmax_rows_kernel(const float* __restrict__ x, int64_t ld_x, int64_t batch,
+                                   int64_t n, const float* __restrict__ taps, int64_t k,
+                                   unsigned* __restrict__ mx) {
+    for (int64_t b = blockIdx.y; b <= batch; b += gridDim.y)
+        absmax_segment(b < batch ? x + b * ld_x : taps, b < batch ? n : k, mx + b);
+}
+
+// 4 floats times 2^e split into two fp16 terms, packed as 4 fp16 (8 bytes) each.
+__device__ __forceinline__ void split4_f16(const float4 v, float scale, uint2 (&out)[3]) {
+    const float s0 = v.x * scale, s1 = v.y * scale, s2 = v.z * scale, s3 = v.w * scale;
+    const __half2 a1 = __floats2half2_rn(s0, s1);
+    const __half2 b1 = __floats2half2_rn(s2, s3);
+    const float2 fa1 = __half22float2(a1), fb1 = __half22float2(b1);
+    const __half2 a2 = __floats2half2_rn(s0 - fa1.x, s1 - fa1.y);
+    const __half2 b2 = __floats2half2_rn(s2 - fb1.x, s3 - fb1.y);
+    out[0].x = *reinterpret_cast<const uint32_t*>(&a1);
+    out[0].y = *reinterpret_cast<const uint32_t*>(&b1);
+    out[1].x = *reinterpret_cast<const uint32_t*>(&a2);
+    out[1].y = *reinterpret_cast<const uint32_t*>(&b2);
+    out[2] = make_uint2(0u, 0u);
+}
+
+// One tap value as its operand terms (bf16: 2 or 3 terms; fp16: 2 terms of
+// v 2^e).
+template <bool F16>
+__device__ __forceinline__ void split_tap(float v, int terms, float scale, op16 (&t)[3]) {
+    if (F16) {
+        const float s = v * scale;
+        const __half h1 = __float2half_rn(s);
+        t[0] = __half_as_ushort(h1);
+        t[1] = __half_as_ushort(__float2half_rn(s - __half2float(h1)));
+        t[2] = 0;
+    } else {
+        const __nv_bfloat16 h1 = __float2bfloat16_rn(v);
+        const float r1 = v - __bfloat162float(h1);
+        const __nv_bfloat16 h2 = __float2bfloat16_rn(r1);
+        t[0] = __bfloat16_as_ushort(h1);
+        t[1] = __bfloat16_as_ushort(h2);
+        t[2] = terms == 3 ? __bfloat16_as_ushort(__float2bfloat16_rn(r1 - __bfloat162float(h2)))
+                          : (op16)0;
+    }
+}
+
+// x -> term planes xs[t][b][i] = term t of x[b][i] (zero for n <= i < nA);
+// FP16X3 scales row b by 2^f16_shift(mx[b]) first.  Each thread converts 4
+// consecutive elements: the loads are coalesced across the warp and each
+// plane gets one 8-byte store.
+template <bool F16>
 __global__ void split_signal_kernel(const float* __restrict__ x, int64_t ld_x, int64_t batch,
                                     int64_t n, int64_t nA, int terms,
-                                    __nv_bfloat16* __restrict__ xs) {
+                                    const unsigned* __restrict__ mx, op16* __restrict__ xs) {
     const int64_t plane = batch * nA;
     const int64_t groups = nA / 4;  // nA is a multiple of 8
     for (int64_t b = blockIdx.y; b < batch; b += gridDim.y) {
         const float* __restrict__ xr = x + b * ld_x;
+        const float scale = F16 ? pow2f(f16_shift(mx[b])) : 1.0f;
         for (int64_t gi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gi < groups;
              gi += (int64_t)gridDim.x * blockDim.x) {
             const int64_t i0 = gi * 4;
@@ -132,7 +218,10 @@ __global__ void split_signal_kernel(const float* __restrict__ x, int64_t ld_x, i
 #pragma unroll
             for (int j = 0; j < 4; ++j) e[j] = i0 + j < n ? __ldg(xr + i0 + j) : 0.0f;
             uint2 t3[3];
-            split4_any(make_float4(e[0], e[1], e[2], e[3]), terms, t3);
+            if (F16)
+                split4_f16(make_float4(e[0], e[1], e[2], e[3]), scale, t3);
+            else
+                split4_any(make_float4(e[0], e[1], e[2], e[3]), terms, t3);
             const int64_t o = b * nA + i0;
 #pragma unroll
             for (int t = 0; t < 3; ++t)
@@ -142,22 +231,25 @@ __global__ void split_signal_kernel(const float* __restrict__ x, int64_t ld_x, i
 }
 
 // Tap operand planes G[t][phi][i] = term t of c[i - 8*(U-1) - phi - m]
-// (zero outside [0, k)), c = taps or reversed taps.
+// (zero outside [0, k)), c = taps or reversed taps (FP16X3: times
+// 2^f16_shift(*mx)).
+template <bool F16>
 __global__ void split_taps_kernel(const float* __restrict__ taps, int64_t k, int reverse, int m,
-                                  int64_t LG, int terms, __nv_bfloat16* __restrict__ G) {
+                                  int64_t LG, int terms, const unsigned* __restrict__ mx,
+                                  op16* __restrict__ G) {
     const int64_t total = (int64_t)kPh * LG;
+    const float scale = F16 ? pow2f(f16_shift(*mx)) : 1.0f;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int ph = (int)(e / LG);
         const int64_t i = e % LG;
         const int64_t ci = i - 8 * (int64_t)(kU - 1) - ph - m;
         const float v = (ci >= 0 && ci < k) ? __ldg(taps + (reverse ? k - 1 - ci : ci)) : 0.0f;
-        const __nv_bfloat16 h1 = __float2bfloat16_rn(v);
-        const float r1 = v - __bfloat162float(h1);
-        const __nv_bfloat16 h2 = __float2bfloat16_rn(r1);
-        G[e] = h1;
-        G[total + e] = h2;
-        if (terms == 3) G[2 * total + e] = __float2bfloat16_rn(r1 - __bfloat162float(h2));
+        op16 t[3];
+        split_tap<F16>(v, terms, scale, t);
+        G[e] = t[0];
+        G[total + e] = t[1];
+        if (terms == 3) G[2 * total + e] = t[2];
     }
 }
 
@@ -190,7 +282,7 @@ __device__ __forceinline__ void live_rows(int64_t J0, int64_t L0, int64_t k, int
 // geometry; ragged launches read it from the plan's tile and signal tables.
 struct TileView {
     const CUtensorMap* map;
-    const __nv_bfloat16* G;
+    const op16* G;
     int64_t LG, k;
     int m, nchunks, pg, vec_store;
     int32_t xc0, row0;   // TMA x coordinate of the first chunk, first row of the box
@@ -198,14 +290,21 @@ struct TileView {
     float* y;            // output row row0 (rows ld apart)
     int64_t ld, o0;      // row stride; output index of column 0 of phase 0 inside a row
     int64_t lim0, dlim;  // outputs past (lim0 - r * dlim) of box row r are not stored
+    const unsigned* mxr;  // FP16X3: max |x| bits of box row r at mxr[r * mxs]
+    int64_t mxs;
+    int shc;              // FP16X3: the taps' scale exponent
 };
 
-template <bool RAGGED>
+template <bool RAGGED, bool F16>
 __device__ __forceinline__ TileView tile_view(int64_t tile, const CUtensorMap* amap,
-                                              const __nv_bfloat16* G, const TcGeom& g, float* y,
+                                              const op16* G, const TcGeom& g, float* y,
                                               int64_t ld_y, const CUtensorMap* maps,
-                                              const TcSig* sigs, const TcTile* tiles) {
+                                              const TcSig* sigs, const TcTile* tiles,
+                                              const unsigned* mx) {
     TileView v;
+    v.mxr = nullptr;
+    v.mxs = 0;
+    v.shc = 0;
     if (RAGGED) {
         const TcTile tt = tiles[tile];
         const TcSig sg = sigs[tt.sig];
@@ -225,6 +324,10 @@ __device__ __forceinline__ TileView tile_view(int64_t tile, const CUtensorMap* a
         v.o0 = (int64_t)tt.blk * kNCOL + kPhT * tt.pg;
         v.lim0 = sg.n_out - (int64_t)tt.row0 * sg.seg;
         v.dlim = sg.seg;
+        if (F16) {  // one signal: every row has its scale
+            v.mxr = mx + 2 * (int64_t)tt.sig;
+            v.shc = f16_shift(mx[2 * (int64_t)tt.sig + 1]);
+        }
     } else {
         const int pg = (int)(tile % kGroups);
         const int64_t w = tile / kGroups;
@@ -245,16 +348,23 @@ __device__ __forceinline__ TileView tile_view(int64_t tile, const CUtensorMap* a
         v.o0 = blk * kNCOL + kPhT * pg;
         v.lim0 = g.n_out;
         v.dlim = 0;
+        if (F16) {
+            v.mxr = mx + v.row0;
+            v.mxs = 1;
+            v.shc = f16_shift(mx[g.batch]);
+        }
     }
     return v;
 }
 
-template <int T, bool RAGGED>  // T bf16 terms per operand: 2 (BF16X3) or 3 (BF16X6)
+// T terms per operand: 2 (BF16X3, FP16X3) or 3 (BF16X6); F16: fp16 terms
+// of scaled operands (FP16X3), else bf16.
+template <int T, bool RAGGED, bool F16>
 __global__ void __launch_bounds__(kThreads, 1)
-fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __restrict__ G,
+fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const op16* __restrict__ G,
               const TcGeom g, float* __restrict__ y, int64_t ld_y, unsigned* __restrict__ err,
               const CUtensorMap* __restrict__ maps, const TcSig* __restrict__ sigs,
-              const TcTile* __restrict__ tiles) {
+              const TcTile* __restrict__ tiles, const unsigned* __restrict__ mx) {
     constexpr int NPROD = T == 2 ? 3 : 6;
     constexpr uint32_t kABytes = T * kABytesTerm;
     extern __shared__ uint8_t smem_raw[];
@@ -294,7 +404,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
             uint32_t it = 0;
             bool ok = true;
             for (int64_t tile = blockIdx.x; ok && tile < g.n_tiles; tile += gridDim.x) {
-                const TileView v = tile_view<RAGGED>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles);
+                const TileView v = tile_view<RAGGED, F16>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles, mx);
                 for (int c = 0; c < v.nchunks; ++c, ++it) {
                     const int st = (int)(it % (uint32_t)g.nstage);
                     const uint32_t ph = (it / (uint32_t)g.nstage) & 1u;
@@ -329,11 +439,13 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issue
         if (lane == 0) {
-            constexpr uint32_t idesc0 = idesc_bf16_f32(kM, 16) & ~(0x3Fu << 17);
+            // A and B formats: bf16 (1) or, for FP16X3, f16 (0)
+            constexpr uint32_t idesc0 =
+                idesc_bf16_f32(kM, 16) & ~(0x3Fu << 17) & (F16 ? ~((1u << 7) | (1u << 10)) : ~0u);
             uint32_t it = 0, tcount = 0;
             bool ok = true;
             for (int64_t tile = blockIdx.x; ok && tile < g.n_tiles; tile += gridDim.x, ++tcount) {
-                const TileView v = tile_view<RAGGED>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles);
+                const TileView v = tile_view<RAGGED, F16>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles, mx);
                 // the epilogue has read (and zeroed) the accumulators of the tile before
                 if (!mbar_wait(tempty, tcount & 1u)) {
                     atomicOr(err, kErrMbarTimeout);
@@ -403,7 +515,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
         mbar_arrive(tempty);
         uint32_t tcount = 0;
         for (int64_t tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++tcount) {
-            const TileView v = tile_view<RAGGED>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles);
+            const TileView v = tile_view<RAGGED, F16>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles, mx);
             if (!mbar_wait(tfull, tcount & 1u)) {
                 if (lane == 0) atomicOr(err, kErrMbarTimeout);
                 break;
@@ -437,6 +549,18 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
             tmem_wait_st();
             tc_fence_before();
             mbar_arrive(tempty);
+            if (F16 && r < v.rows) {
+                // undo the scales 2^(e+f) of the row and the taps (two exact
+                // power-of-two multiplies)
+                const int sh = f16_shift(v.mxr[r * v.mxs]) + v.shc;
+                const float f1 = pow2f(-(sh / 2)), f2 = pow2f(-(sh - sh / 2));
+#pragma unroll
+                for (int gi = 0; gi < kGrp; ++gi)
+#pragma unroll
+                    for (int l = 0; l < kPhT; ++l)
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) out[gi][l][i] = out[gi][l][i] * f1 * f2;
+            }
             if (r < v.rows) {
 #pragma unroll
                 for (int gi = 0; gi < kGrp; ++gi) {
@@ -467,7 +591,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __r
     }
 }
 
-template <int T>
+template <int T, bool F16>
 int launch_tc(const FirArgs& a, cudaStream_t st) {
     const DeviceInfo* info = nullptr;
     int rc = current_device(&info);
@@ -503,33 +627,42 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
     const size_t smem = (size_t)nstage * g.stage_bytes + extra;
 
     // the signal's term planes and the tap operand planes into scratch memory
-    __nv_bfloat16* xs = nullptr;
-    __nv_bfloat16* Gs = nullptr;
-    const size_t xs_bytes = sizeof(__nv_bfloat16) * (size_t)T * (size_t)a.batch * (size_t)nA;
-    const size_t g_bytes = sizeof(__nv_bfloat16) * (size_t)T * kPh * (size_t)g.LG;
+    // (FP16X3: and the max |x| of every row and of the taps)
+    op16* xs = nullptr;
+    op16* Gs = nullptr;
+    unsigned* mx = nullptr;
+    const size_t xs_bytes = sizeof(op16) * (size_t)T * (size_t)a.batch * (size_t)nA;
+    const size_t g_bytes = sizeof(op16) * (size_t)T * kPh * (size_t)g.LG;
     rc = scratch_alloc((void**)&xs, xs_bytes, st);
-    if (rc) return rc;
-    rc = scratch_alloc((void**)&Gs, g_bytes, st);
-    if (rc) {
-        scratch_free(xs, st);
-        return rc;
-    }
+    if (!rc) rc = scratch_alloc((void**)&Gs, g_bytes, st);
+    if (!rc && F16) rc = scratch_alloc((void**)&mx, sizeof(unsigned) * (size_t)(a.batch + 1), st);
     CUtensorMap amap;
-    rc = make_tmap_3d(&amap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, xs, (uint64_t)nA, (uint64_t)a.batch,
-                      (uint64_t)T, (uint64_t)nA * 2, (uint64_t)nA * 2 * (uint64_t)a.batch, kKC, kM,
-                      1, CU_TENSOR_MAP_SWIZZLE_128B);
+    if (!rc)
+        rc = make_tmap_3d(&amap, F16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                          xs, (uint64_t)nA, (uint64_t)a.batch, (uint64_t)T, (uint64_t)nA * 2,
+                          (uint64_t)nA * 2 * (uint64_t)a.batch, kKC, kM, 1,
+                          CU_TENSOR_MAP_SWIZZLE_128B);
     if (rc == SCIR_OK) {
         const unsigned gx = (unsigned)std::min<int64_t>(ceil_div(nA / 4, 256), 4096);
         const unsigned gy = (unsigned)std::min<int64_t>(a.batch, 65535);
-        split_signal_kernel<<<dim3(gx, gy), 256, 0, st>>>(a.x, a.ld_x, a.batch, a.n, nA, T, xs);
+        if (F16) {
+            cudaError_t me = cudaMemsetAsync(mx, 0, sizeof(unsigned) * (size_t)(a.batch + 1), st);
+            if (me != cudaSuccess) rc = set_error(SCIR_ERR_CUDA, "max reset: %s", cudaGetErrorString(me));
+            const unsigned mxg = (unsigned)std::min<int64_t>(ceil_div(a.n, 1024), 64);
+            absmax_rows_kernel<<<dim3(mxg, (unsigned)std::min<int64_t>(a.batch + 1, 65535)), 256, 0,
+                                 st>>>(a.x, a.ld_x, a.batch, a.n, a.taps, a.k, mx);
+        }
+        split_signal_kernel<F16><<<dim3(gx, gy), 256, 0, st>>>(a.x, a.ld_x, a.batch, a.n, nA, T,
+                                                               mx, xs);
         const unsigned gt = (unsigned)std::min<int64_t>(ceil_div((int64_t)kPh * g.LG, 256), 4096);
-        split_taps_kernel<<<gt, 256, 0, st>>>(a.taps, a.k, a.reverse, g.m, g.LG, T, Gs);
+        split_taps_kernel<F16><<<gt, 256, 0, st>>>(a.taps, a.k, a.reverse, g.m, g.LG, T,
+                                                   F16 ? mx + a.batch : nullptr, Gs);
         cudaError_t le = cudaGetLastError();
         if (le != cudaSuccess)
             rc = set_error(SCIR_ERR_CUDA, "split kernels: %s", cudaGetErrorString(le));
     }
     if (rc == SCIR_OK) {
-        auto kern = fir_tc_kernel<T, false>;
+        auto kern = fir_tc_kernel<T, false, F16>;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) {
@@ -539,7 +672,7 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
         } else {
             const int64_t grid = std::min<int64_t>(g.n_tiles, (int64_t)info->sm_count);
             kern<<<(unsigned)grid, kThreads, smem, st>>>(amap, Gs, g, a.y, a.ld_y, err, nullptr,
-                                                         nullptr, nullptr);
+                                                         nullptr, nullptr, mx);
             cudaError_t le = cudaGetLastError();
             if (le != cudaSuccess)
                 rc = set_error(SCIR_ERR_CUDA, "launch of fir_tc_kernel failed: %s",
@@ -548,6 +681,7 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
     }
     scratch_free(xs, st);
     scratch_free(Gs, st);
+    scratch_free(mx, st);
     return rc;
 }
 
@@ -558,13 +692,28 @@ struct TcSplit {
     int32_t reverse, m;
 };
 
-// Signal i's planes: element pad_front + j holds term t of x_i[j], zero
-// elsewhere in its region (the history before the signal and the tail).
+// FP16X3: mx[2i] = max |x_i| bits, mx[2i + 1] = max |taps_i| bits (blockIdx.z
+// picks which; mx zeroed).
+__global__ void absmax_ragged_kernel(const TcSplit* __restrict__ sp, const float* __restrict__ x,
+                                     const float* __restrict__ taps, unsigned* __restrict__ mx) {
+    const TcSplit d = sp[blockIdx.y];
+    if (blockIdx.z == 0)
+        absmax_segment(x + d.x_off, d.n, mx + 2 * (int64_t)blockIdx.y);
+    else
+        absmax_segment(taps + d.taps_off, d.k, mx + 2 * (int64_t)blockIdx.y + 1);
+}
+
+// Signal i's planes: element pad_front + j holds term t of x_i[j] (FP16X3:
+// of x_i[j] 2^e_i), zero elsewhere in its region (the history before the
+// signal and the tail).
+template <bool F16>
 __global__ void split_planes_ragged_kernel(const TcSplit* __restrict__ sp, const float* __restrict__ x,
                                            int64_t plane_len, int terms,
-                                           __nv_bfloat16* __restrict__ planes) {
+                                           const unsigned* __restrict__ mx,
+                                           op16* __restrict__ planes) {
     const TcSplit d = sp[blockIdx.y];
     const float* __restrict__ xs = x + d.x_off;
+    const float scale = F16 ? pow2f(f16_shift(mx[2 * (int64_t)blockIdx.y])) : 1.0f;
     for (int64_t e0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4; e0 < d.region;
          e0 += (int64_t)gridDim.x * blockDim.x * 4) {
         float v[4];
@@ -574,7 +723,10 @@ __global__ void split_planes_ragged_kernel(const TcSplit* __restrict__ sp, const
             v[j] = (src >= 0 && src < d.n) ? __ldg(xs + src) : 0.0f;
         }
         uint2 t3[3];
-        split4_any(make_float4(v[0], v[1], v[2], v[3]), terms, t3);
+        if (F16)
+            split4_f16(make_float4(v[0], v[1], v[2], v[3]), scale, t3);
+        else
+            split4_any(make_float4(v[0], v[1], v[2], v[3]), terms, t3);
 #pragma unroll
         for (int t = 0; t < 3; ++t)
             if (t < terms)
@@ -582,12 +734,16 @@ __global__ void split_planes_ragged_kernel(const TcSplit* __restrict__ sp, const
     }
 }
 
-// Signal i's tap planes G_i[t][phi][e] = term t of c[e - 8*(U-1) - phi - m].
+// Signal i's tap planes G_i[t][phi][e] = term t of c[e - 8*(U-1) - phi - m]
+// (FP16X3: of c 2^f_i).
+template <bool F16>
 __global__ void split_taps_ragged_kernel(const TcSplit* __restrict__ sp, const float* __restrict__ taps,
-                                         int terms, __nv_bfloat16* __restrict__ G) {
+                                         int terms, const unsigned* __restrict__ mx,
+                                         op16* __restrict__ G) {
     const TcSplit d = sp[blockIdx.y];
     const int64_t total = (int64_t)kPh * d.LG;
-    __nv_bfloat16* Gi = G + d.g_off;
+    op16* Gi = G + d.g_off;
+    const float scale = F16 ? pow2f(f16_shift(mx[2 * (int64_t)blockIdx.y + 1])) : 1.0f;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int ph = (int)(e / d.LG);
@@ -596,12 +752,11 @@ __global__ void split_taps_ragged_kernel(const TcSplit* __restrict__ sp, const f
         const float v = (ci >= 0 && ci < d.k)
                             ? __ldg(taps + d.taps_off + (d.reverse ? d.k - 1 - ci : ci))
                             : 0.0f;
-        const __nv_bfloat16 h1 = __float2bfloat16_rn(v);
-        const float r1 = v - __bfloat162float(h1);
-        const __nv_bfloat16 h2 = __float2bfloat16_rn(r1);
-        Gi[e] = h1;
-        Gi[total + e] = h2;
-        if (terms == 3) Gi[2 * total + e] = __float2bfloat16_rn(r1 - __bfloat162float(h2));
+        op16 t[3];
+        split_tap<F16>(v, terms, scale, t);
+        Gi[e] = t[0];
+        Gi[total + e] = t[1];
+        if (terms == 3) Gi[2 * total + e] = t[2];
     }
 }
 
@@ -628,10 +783,11 @@ bool fir_tc_supported(const FirArgs& a) {
 // ------------------------------------------------------------------ ragged bucket
 
 struct TcRaggedPlan {
-    int terms = 3;
+    int form = kTcBf16x6, terms = 3;
     int64_t nsig = 0, ntiles = 0, plane_len = 0, g_len = 0;
-    __nv_bfloat16* planes = nullptr;
-    __nv_bfloat16* G = nullptr;
+    op16* planes = nullptr;
+    op16* G = nullptr;
+    unsigned* mx = nullptr;  // FP16X3: max |x_i|, max |taps_i| bits per signal
     CUtensorMap* maps = nullptr;
     TcSig* sigs = nullptr;
     TcTile* tiles = nullptr;
@@ -647,15 +803,18 @@ void tc_ragged_destroy(TcRaggedPlan* p) {
     cudaFree(p->sigs);
     cudaFree(p->tiles);
     cudaFree(p->split);
+    cudaFree(p->mx);
     delete p;
 }
 
 int64_t tc_ragged_tiles(const TcRaggedPlan* p) { return p ? p->ntiles : 0; }
 
-int tc_ragged_create(const TcSigIn* in, int64_t count, int terms, TcRaggedPlan** out) {
+int tc_ragged_create(const TcSigIn* in, int64_t count, int form, TcRaggedPlan** out) {
     *out = nullptr;
     if (count == 0) return SCIR_OK;
     auto p = new TcRaggedPlan();
+    const int terms = form == kTcBf16x6 ? 3 : 2;
+    p->form = form;
     p->terms = terms;
     p->nsig = count;
     std::vector<TcSig> sig((size_t)count);
@@ -732,8 +891,10 @@ int tc_ragged_create(const TcSigIn* in, int64_t count, int terms, TcRaggedPlan**
         tc_ragged_destroy(p);
         return code;
     };
-    cudaError_t e = cudaMalloc(&p->planes, sizeof(__nv_bfloat16) * (size_t)terms * (size_t)p->plane_len);
-    if (e == cudaSuccess) e = cudaMalloc(&p->G, sizeof(__nv_bfloat16) * (size_t)p->g_len);
+    cudaError_t e = cudaMalloc(&p->planes, sizeof(op16) * (size_t)terms * (size_t)p->plane_len);
+    if (e == cudaSuccess) e = cudaMalloc(&p->G, sizeof(op16) * (size_t)p->g_len);
+    if (e == cudaSuccess && form == kTcFp16x3)
+        e = cudaMalloc(&p->mx, sizeof(unsigned) * 2 * (size_t)count);
     if (e == cudaSuccess) e = cudaMalloc(&p->maps, sizeof(CUtensorMap) * (size_t)count);
     if (e == cudaSuccess) e = cudaMalloc(&p->sigs, sizeof(TcSig) * (size_t)count);
     if (e == cudaSuccess) e = cudaMalloc(&p->tiles, sizeof(TcTile) * sorted.size());
@@ -748,7 +909,9 @@ int tc_ragged_create(const TcSigIn* in, int64_t count, int terms, TcRaggedPlan**
         const TcSig& S = sig[(size_t)i];
         const TcSplit& P = sp[(size_t)i];
         const int64_t X = (int64_t)S.x0 + (S.seg / kNCOL - 1) * kNCOL + (int64_t)S.nchunks * kKC;
-        const int rc = make_tmap_3d(&maps[(size_t)i], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+        const int rc = make_tmap_3d(&maps[(size_t)i],
+                                    form == kTcFp16x3 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                      : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
                                     p->planes + P.plane_off, (uint64_t)X, (uint64_t)S.rows,
                                     (uint64_t)terms, (uint64_t)S.seg * 2,
                                     (uint64_t)p->plane_len * 2, kKC, kM, 1,
@@ -764,7 +927,7 @@ int tc_ragged_create(const TcSigIn* in, int64_t count, int terms, TcRaggedPlan**
     return SCIR_OK;
 }
 
-template <int T>
+template <int T, bool F16>
 int tc_ragged_launch(const TcRaggedPlan* p, float* y, const DeviceInfo* info, unsigned* err,
                      cudaStream_t st) {
     TcGeom g{};
@@ -773,13 +936,13 @@ int tc_ragged_launch(const TcRaggedPlan* p, float* y, const DeviceInfo* info, un
     if (rc) return rc;
     g.n_tiles = p->ntiles;
     g.vec_store = (reinterpret_cast<uintptr_t>(y) & 7) == 0 ? 1 : 0;
-    auto kern = fir_tc_kernel<T, true>;
+    auto kern = fir_tc_kernel<T, true, F16>;
     SCIR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CUtensorMap unused;
     memset(&unused, 0, sizeof(unused));
     const int64_t grid = std::min<int64_t>(p->ntiles, (int64_t)info->sm_count);
     kern<<<(unsigned)grid, kThreads, smem, st>>>(unused, p->G, g, y, 0, err, p->maps, p->sigs,
-                                                 p->tiles);
+                                                 p->tiles, p->mx);
     SCIR_LAUNCH_CHECK("fir_tc_kernel (ragged)");
     return SCIR_OK;
 }
@@ -793,21 +956,39 @@ int tc_ragged_run(const TcRaggedPlan* p, const float* x, const float* taps, floa
     unsigned* err = device_error_word();
     if (!err) return set_error(SCIR_ERR_CUDA, "device error word unavailable");
     SCIR_REQUIRE(p->nsig <= 65535, SCIR_ERR_UNSUPPORTED, "more than 65,535 tensor-core signals");
+    const bool f16 = p->form == kTcFp16x3;
+    if (f16) {
+        SCIR_CUDA_TRY(cudaMemsetAsync(p->mx, 0, sizeof(unsigned) * 2 * (size_t)p->nsig, st));
+        const unsigned bm = (unsigned)std::min<int64_t>(ceil_div(p->max_region, 1024), 64);
+        absmax_ragged_kernel<<<dim3(bm, (unsigned)p->nsig, 2), 256, 0, st>>>(p->split, x, taps, p->mx);
+    }
     const unsigned bx = (unsigned)std::min<int64_t>(ceil_div(p->max_region / 4, 256), 256);
-    split_planes_ragged_kernel<<<dim3(bx, (unsigned)p->nsig), 256, 0, st>>>(
-        p->split, x, p->plane_len, p->terms, p->planes);
     const unsigned bt = (unsigned)std::min<int64_t>(ceil_div(p->max_g, 256), 64);
-    split_taps_ragged_kernel<<<dim3(bt, (unsigned)p->nsig), 256, 0, st>>>(p->split, taps, p->terms,
-                                                                           p->G);
+    if (f16) {
+        split_planes_ragged_kernel<true><<<dim3(bx, (unsigned)p->nsig), 256, 0, st>>>(
+            p->split, x, p->plane_len, p->terms, p->mx, p->planes);
+        split_taps_ragged_kernel<true><<<dim3(bt, (unsigned)p->nsig), 256, 0, st>>>(
+            p->split, taps, p->terms, p->mx, p->G);
+    } else {
+        split_planes_ragged_kernel<false><<<dim3(bx, (unsigned)p->nsig), 256, 0, st>>>(
+            p->split, x, p->plane_len, p->terms, nullptr, p->planes);
+        split_taps_ragged_kernel<false><<<dim3(bt, (unsigned)p->nsig), 256, 0, st>>>(
+            p->split, taps, p->terms, nullptr, p->G);
+    }
     SCIR_LAUNCH_CHECK("ragged split kernels");
-    return p->terms == 2 ? tc_ragged_launch<2>(p, y, info, err, st)
-                         : tc_ragged_launch<3>(p, y, info, err, st);
+    if (f16) return tc_ragged_launch<2, true>(p, y, info, err, st);
+    return p->terms == 2 ? tc_ragged_launch<2, false>(p, y, info, err, st)
+                         : tc_ragged_launch<3, false>(p, y, info, err, st);
 }
 
-int launch_fir_tc(const FirArgs& a, int terms, cudaStream_t st) {
+int launch_fir_tc(const FirArgs& a, int form, cudaStream_t st) {
     if (a.batch == 0 || a.n_out == 0) return SCIR_OK;
-    if (terms == 2) return launch_tc<2>(a, st);
-    return launch_tc<3>(a, st);
+    switch (form) {
+    case kTcBf16x3: return launch_tc<2, false>(a, st);
+    case kTcBf16x6: return launch_tc<3, false>(a, st);
+    case kTcFp16x3: return launch_tc<2, true>(a, st);
+    default: return set_error(SCIR_ERR_INVALID_ARG, "unknown tensor-core form %d", form);
+    }
 }
 
 }  // namespace scir

@@ -25,7 +25,10 @@ int fir_geometry(int64_t n, int64_t k, int mode, int* reverse, int64_t* s, int64
 // v: outputs per thread (8 or 16), 0 = by tap count.
 int launch_fir_simt(const FirArgs& a, bool exact, cudaStream_t st, int v = 0);
 // Tensor-core (tcgen05) FIR with split-bf16 operands; terms = 2 (BF16X3) or 3 (BF16X6).
-int launch_fir_tc(const FirArgs& a, int terms, cudaStream_t st);
+// Operand forms of the tensor-core FIR: two or three bf16 terms, or two fp16
+// terms of power-of-two scaled operands.
+enum TcForm : int { kTcBf16x3 = 2, kTcBf16x6 = 3, kTcFp16x3 = 4 };
+int launch_fir_tc(const FirArgs& a, int form, cudaStream_t st);
 bool fir_tc_supported(const FirArgs& a);
 
 // Tensor-core bucket of a ragged plan (fir_tc.cu).  Each signal is tiled as
@@ -49,7 +52,7 @@ struct TcSigIn {       // one signal as the ragged plan describes it
     int reverse;
 };
 struct TcRaggedPlan;
-int tc_ragged_create(const TcSigIn* sigs, int64_t count, int terms, TcRaggedPlan** out);
+int tc_ragged_create(const TcSigIn* sigs, int64_t count, int form, TcRaggedPlan** out);
 void tc_ragged_destroy(TcRaggedPlan* p);
 int64_t tc_ragged_tiles(const TcRaggedPlan* p);
 int tc_ragged_run(const TcRaggedPlan* p, const float* x, const float* taps, float* y,

@@ -30,9 +30,10 @@ struct RaggedTile {
 
 struct scir_ragged_plan {
     int device = -1, mode = 0, precision = 0;
-    // tensor-core bucket: signals with at least tc_min_taps taps (AUTO, BF16X3,
-    // BF16X6) run the split-bf16 tensor-core contraction in its own launch
-    int tc_terms = 0, tc_min_taps = 1 << 30;
+    // tensor-core bucket: signals with at least tc_min_taps taps (AUTO,
+    // FP16X3, BF16X3, BF16X6) run the split-operand tensor-core contraction
+    // in its own launch; tc_form is its scir::TcForm (0: no bucket)
+    int tc_form = 0, tc_min_taps = 1 << 30;
     std::vector<char> in_tc;          // per signal
     scir::TcRaggedPlan* tc = nullptr;
     int64_t count = 0, ntiles = 0, samples_in = 0;
@@ -139,7 +140,7 @@ int build_tc(scir_ragged_plan* p, int min_taps) {
     p->tc = nullptr;
     p->in_tc.assign(p->h_sigs.size(), 0);
     p->tc_min_taps = min_taps;
-    if (p->tc_terms == 0) return build_tiles(p, p->v16_min_taps);
+    if (p->tc_form == 0) return build_tiles(p, p->v16_min_taps);
     std::vector<TcSigIn> in;
     for (size_t i = 0; i < p->h_sigs.size(); ++i) {
         const RaggedSig& s = p->h_sigs[i];
@@ -147,7 +148,7 @@ int build_tc(scir_ragged_plan* p, int min_taps) {
         p->in_tc[i] = 1;
         in.push_back(TcSigIn{s.x_off, s.n, s.taps_off, s.k, s.y_off, s.s, s.n_out, s.reverse});
     }
-    int rc = tc_ragged_create(in.data(), (int64_t)in.size(), p->tc_terms, &p->tc);
+    int rc = tc_ragged_create(in.data(), (int64_t)in.size(), p->tc_form, &p->tc);
     if (rc) return rc;
     return build_tiles(p, p->v16_min_taps);
 }
@@ -164,12 +165,13 @@ SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count
     *plan = nullptr;
     SCIR_REQUIRE(count >= 0 && (count == 0 || desc), SCIR_ERR_INVALID_ARG, "bad descriptor table");
     SCIR_REQUIRE(count < (1LL << 31), SCIR_ERR_UNSUPPORTED, "too many signals");
-    // AUTO, BF16X6, BF16X3: long filters on the tensor cores (split-bf16 with
-    // three or two terms), the rest in FP32 on the CUDA cores
-    int tc_terms = 0;
-    if (precision == SCIR_PREC_AUTO || precision == SCIR_PREC_BF16X6) tc_terms = 3;
-    if (precision == SCIR_PREC_BF16X3) tc_terms = 2;
-    if (tc_terms) precision = SCIR_PREC_FP32;
+    // AUTO (FP16X3), FP16X3, BF16X6, BF16X3: long filters on the tensor
+    // cores, the rest in FP32 on the CUDA cores
+    int tc_form = 0;
+    if (precision == SCIR_PREC_AUTO || precision == SCIR_PREC_FP16X3) tc_form = scir::kTcFp16x3;
+    if (precision == SCIR_PREC_BF16X6) tc_form = scir::kTcBf16x6;
+    if (precision == SCIR_PREC_BF16X3) tc_form = scir::kTcBf16x3;
+    if (tc_form) precision = SCIR_PREC_FP32;
     SCIR_REQUIRE(precision == SCIR_PREC_FP32 || precision == SCIR_PREC_REF_EXACT,
                  SCIR_ERR_UNSUPPORTED, "unknown ragged precision");
     const DeviceInfo* info = nullptr;
@@ -180,7 +182,7 @@ SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count
     p->device = info->device;
     p->mode = mode;
     p->precision = precision;
-    p->tc_terms = tc_terms;
+    p->tc_form = tc_form;
     p->count = count;
     std::vector<RaggedSig> sigs((size_t)count);
     for (int64_t i = 0; i < count; ++i) {
@@ -236,7 +238,7 @@ SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count
         return fail(SCIR_ERR_CUDA);
     }
     p->per_sm = per_sm;
-    rc = build_tc(p, tc_terms ? 512 : (1 << 30));
+    rc = build_tc(p, tc_form ? 512 : (1 << 30));
     if (rc) return fail(rc);
     *plan = p;
     return SCIR_OK;
@@ -330,7 +332,7 @@ SCIR_API int scir_ragged_plan_autotune(scir_ragged_plan* plan, const float* x, c
     }
     if (!rc) rc = build_tiles(plan, best);
     // 2. the tap count from which signals go to the tensor cores
-    if (!rc && plan->tc_terms) {
+    if (!rc && plan->tc_form) {
         static const int kTc[] = {256, 512, 1024, 2048, 1 << 30};
         int best_tc = plan->tc_min_taps;
         float best_tc_t = 0.0f;
@@ -361,7 +363,7 @@ SCIR_API int scir_ragged_plan_tensor_cores(const scir_ragged_plan* plan, int* mi
     SCIR_REQUIRE(plan != nullptr, SCIR_ERR_INVALID_ARG, "plan is NULL");
     int64_t cnt = 0;
     for (char c : plan->in_tc) cnt += c ? 1 : 0;
-    if (min_taps) *min_taps = plan->tc_terms ? plan->tc_min_taps : 0;
+    if (min_taps) *min_taps = plan->tc_form ? plan->tc_min_taps : 0;
     if (signals) *signals = cnt;
     return SCIR_OK;
 }

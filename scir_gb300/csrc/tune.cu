@@ -3,8 +3,8 @@
 // shape.
 //
 //   FIR (REF_EXACT / FP32 / AUTO precision): CUDA-core tiles of 8 or 16
-//     outputs per thread; with AUTO also the tensor-core BF16X6 path (the
-//     only other form that holds 1e-5).  The default without tuning is 16
+//     outputs per thread; with AUTO also the tensor-core FP16X3 path (a
+//     tensor-core form that holds 1e-5 at three products).  The default without tuning is 16
 //     from 128 taps on and the tensor cores from 512 taps on.
 //   resample_poly / upfirdn: outputs per lane P (from the minimum that keeps
 //     a period within one warp up to 5) and channels per work item (1, 2 or
@@ -133,7 +133,7 @@ void put_choice(char* buf, size_t len, const std::string& s) {
 }
 
 const char* fir_choice_name(int c) {
-    return c == 1 ? "cuda-cores-v8" : c == 2 ? "cuda-cores-v16" : c == 3 ? "tensor-cores-bf16x6" : "default";
+    return c == 1 ? "cuda-cores-v8" : c == 2 ? "cuda-cores-v16" : c == 3 ? "tensor-cores-fp16x3" : "default";
 }
 
 }  // namespace
@@ -207,7 +207,7 @@ SCIR_API int scir_autotune_fir(int64_t batch, int64_t n, int64_t k, int mode, in
         float t = 0.0f;
         rc = time_calls(
             [&]() -> int {
-                return c == 3 ? launch_fir_tc(a, 3, st) : launch_fir_simt(a, exact, st, c == 1 ? 8 : 16);
+                return c == 3 ? launch_fir_tc(a, kTcFp16x3, st) : launch_fir_simt(a, exact, st, c == 1 ? 8 : 16);
             },
             st, 3, &t);
         if (!rc && (best == 0 || t < best_t)) {

@@ -129,14 +129,18 @@ def test_host_pipeline_many_chunks(cuda):
 
 
 # ---------------------------------------------------------------- tensor cores
-# BF16X6 (three bf16 terms, six products) must meet the FP32 bound of 1e-5;
-# BF16X3 (hi+lo, three products) carries ~16 significant bits per product and
-# is held to a stated bound of 3e-5 normwise (about 7e-6 on the long-tap
-# band-pass workload).
+# BF16X6 (three bf16 terms, six products) and FP16X3 (scaled fp16 hi+lo,
+# three products, 22 significant bits per operand) must meet the FP32 bound
+# of 1e-5; BF16X3 (bf16 hi+lo, three products) carries ~16 significant bits
+# per product and is held to a stated bound of 3e-5 normwise (about 7e-6 on
+# the long-tap band-pass workload).
 TOL_BF16X3 = 3e-5
+TC_FORMS = [(S.Precision.FP16X3, TOL_FP32), (S.Precision.BF16X6, TOL_FP32),
+            (S.Precision.BF16X3, TOL_BF16X3)]
+TC_TOL = dict(TC_FORMS)
 
 
-@pytest.mark.parametrize("prec,tol", [(S.Precision.BF16X6, TOL_FP32), (S.Precision.BF16X3, TOL_BF16X3)])
+@pytest.mark.parametrize("prec,tol", TC_FORMS, ids=lambda v: getattr(v, "name", str(v)))
 @pytest.mark.parametrize("mode", list(S.FirMode))
 @pytest.mark.parametrize("b,n,k", [(3, 1000, 63), (130, 3000, 700), (2, 40000, 4095), (1, 300, 1)])
 def test_tensor_core_vs_fp64(cuda, prec, tol, mode, b, n, k):
@@ -168,12 +172,47 @@ def test_tensor_core_cfg3_bandpass(cuda):
     rows = [0, 1, 64, 127, 128, 129]
     ref = O.fir_mode_f64(x[rows].astype(np.float64), taps.astype(np.float64), int(S.FirMode.LFILTER))
     xd, td = _dev(x, cuda), _dev(taps, cuda)
-    for prec in (S.Precision.BF16X3, S.Precision.BF16X6):
+    for prec in (S.Precision.BF16X3, S.Precision.BF16X6, S.Precision.FP16X3, S.Precision.AUTO):
         y = S.fir_batched(xd, td, S.FirMode.LFILTER, prec).cpu().numpy()
         assert normwise_err(y[rows], ref) < 1e-5, prec
 
 
-@pytest.mark.parametrize("prec", [S.Precision.BF16X3, S.Precision.BF16X6])
+def test_fp16x3_scaling(cuda):
+    # FP16X3 scales every row (and the taps) by a power of two from its
+    # largest finite magnitude: rows of 1e6 and 1e-20 in one batch, an
+    # all-zero row, taps of 1e-4 scale; each row is held to 1e-5 of itself
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-1, 1, (6, 20000))
+    x[1] *= 1e6
+    x[2] *= 1e-20
+    x[3] = 0.0
+    x[4, ::7] *= 1e3  # a row whose largest samples sit on a sparse comb
+    x = x.astype(np.float32)
+    taps = (rng.standard_normal(1500) * 1e-4).astype(np.float32)
+    ref = O.fir_mode_f64(x.astype(np.float64), taps.astype(np.float64), int(S.FirMode.LFILTER))
+    y = S.fir_batched(_dev(x, cuda), _dev(taps, cuda), S.FirMode.LFILTER,
+                      S.Precision.FP16X3).cpu().numpy()
+    assert np.all(y[3] == 0.0)
+    for r in (0, 1, 2, 4, 5):
+        assert normwise_err(y[r], ref[r]) < TOL_FP32, r
+
+
+@pytest.mark.parametrize("prec", [S.Precision.FP16X3, S.Precision.BF16X6, S.Precision.FP32])
+def test_tensor_core_dc_lowpass(cuda, prec):
+    # a constant input through a low-pass filter with positive taps: every
+    # partial sum grows the same way, so a rounding bias in the accumulation
+    # would add up instead of cancelling
+    x = np.ones((4, 30000), np.float32)
+    x[1] = 0.75
+    x[2, :] = np.linspace(0.5, 1.0, 30000, dtype=np.float32)
+    x[3] = 3.0
+    taps = ss.firwin(4095, 0.01).astype(np.float32)
+    ref = O.fir_mode_f64(x.astype(np.float64), taps.astype(np.float64), int(S.FirMode.LFILTER))
+    y = S.fir_batched(_dev(x, cuda), _dev(taps, cuda), S.FirMode.LFILTER, prec).cpu().numpy()
+    assert normwise_err(y, ref) < TOL_FP32
+
+
+@pytest.mark.parametrize("prec", [S.Precision.BF16X3, S.Precision.BF16X6, S.Precision.FP16X3])
 @pytest.mark.parametrize("k", [2, 3, 16, 17, 64, 1025])
 def test_tensor_core_unaligned_rows(cuda, prec, k):
     # x starting one float past a 16-byte boundary (scalar signal loads), an
@@ -188,8 +227,7 @@ def test_tensor_core_unaligned_rows(cuda, prec, k):
     ref = O.fir_mode_f64(big[:, 1:2501].astype(np.float64), taps.astype(np.float64),
                          int(S.FirMode.LFILTER))
     S.fir_batched(xd, _dev(taps, cuda), S.FirMode.LFILTER, prec, out=out)
-    tol = TOL_FP32 if prec == S.Precision.BF16X6 else TOL_BF16X3
-    assert normwise_err(out.cpu().numpy(), ref) < tol
+    assert normwise_err(out.cpu().numpy(), ref) < TC_TOL[prec]
 
 
 def test_tensor_core_strided_and_repeat(cuda):

@@ -183,6 +183,10 @@ def test_resample_tc_refuses_unserved_shape(cuda):
     x = np.zeros((4, 1001), np.float32)
     with pytest.raises(S.GpuError):
         S.resample_poly_f32(_dev(x, cuda), 160, 147, precision=S.Precision.BF16X3)
+    # FP16X3 is a form of the FIR entry points only
+    x = np.zeros((4, 1024), np.float32)
+    with pytest.raises(S.GpuError):
+        S.resample_poly_f32(_dev(x, cuda), 160, 147, precision=S.Precision.FP16X3)
 
 
 def test_resample_tc_cfg2_full_size(cuda):

@@ -102,8 +102,8 @@ def test_library_graph_capture_mixed_calls(cuda):
     plan.close()
 
 
-# ------------------------------------------ tensor-core bucket (AUTO, BF16X6 / BF16X3)
-# Signals with >= 512 taps and >= 16,384 outputs run the split-bf16
+# ------------------------------- tensor-core bucket (AUTO = FP16X3, BF16X6, BF16X3)
+# Signals with >= 512 taps and >= 16,384 outputs run the split-operand
 # contraction as segment rows (up to 128 per signal) in their own persistent
 # launch; the rest stay on the CUDA cores.  Both buckets are checked against
 # the FP64 oracle, with odd output offsets (scalar stores) among them.
@@ -118,7 +118,8 @@ def _mixed_set(seed, count):
     return n, k, x, taps
 
 
-@pytest.mark.parametrize("prec,tol", [(S.Precision.AUTO, 1e-5), (S.Precision.BF16X3, 3e-5)])
+@pytest.mark.parametrize("prec,tol", [(S.Precision.AUTO, 1e-5), (S.Precision.BF16X6, 1e-5),
+                                      (S.Precision.BF16X3, 3e-5)])
 @pytest.mark.parametrize("mode", [S.FirMode.LFILTER, S.FirMode.REF_CORR, S.FirMode.FULL,
                                   S.FirMode.VALID])
 def test_ragged_tensor_core_bucket(cuda, prec, tol, mode):
@@ -141,6 +142,33 @@ def test_ragged_tensor_core_bucket(cuda, prec, tol, mode):
         ref = O.fir_mode_f64(xi, ti, int(mode))[0]
         yi = y[y_off[i]:y_off[i] + n_out[i]]
         assert normwise_err(yi, ref) < tol, (i, int(n[i]), int(k[i]))
+    plan.close()
+
+
+def test_ragged_fp16x3_per_signal_scale(cuda):
+    # every tensor-core signal has its own power-of-two scales (signal and
+    # taps): magnitudes from 1e-15 to 1e6 side by side, one signal all zero
+    import torch
+    n, k, x, taps = _mixed_set(77, 12)
+    scale = np.array([1e6, 1e-15, 0.0, 3e-3, 1.0, 1e4, 1.0, 2e-8, 1.0, 1.0, 5.0, 1.0])
+    tscale = np.array([1.0, 1e3, 1.0, 1e-6, 1.0, 1.0, 1e-9, 1.0, 1.0, 7.0, 1.0, 1.0])
+    plan = S.RaggedPlan(n, k, S.FirMode.LFILTER, S.Precision.FP16X3)
+    for i in range(len(n)):
+        x[plan.x_off[i]:plan.x_off[i] + n[i]] *= np.float32(scale[i])
+        taps[plan.taps_off[i]:plan.taps_off[i] + k[i]] *= np.float32(tscale[i])
+    assert plan.tensor_cores()[1] >= 3
+    y = torch.full((plan.y_len,), float("nan"), device=cuda)
+    plan.run(torch.from_numpy(x).to(cuda), torch.from_numpy(taps).to(cuda), y)
+    y = y.cpu().numpy()
+    for i in range(len(n)):
+        xi = x[plan.x_off[i]:plan.x_off[i] + n[i]].astype(np.float64)
+        ti = taps[plan.taps_off[i]:plan.taps_off[i] + k[i]].astype(np.float64)
+        ref = O.fir_mode_f64(xi, ti, int(S.FirMode.LFILTER))[0]
+        yi = y[plan.y_off[i]:plan.y_off[i] + n[i]]
+        if scale[i] == 0.0:
+            assert np.all(yi == 0.0)
+        else:
+            assert normwise_err(yi, ref) < 1e-5, (i, int(n[i]), int(k[i]))
     plan.close()
 
 
