@@ -571,13 +571,16 @@ class Ragged(Workload):
 
     def floor_ms(self, fp32_tflops, bf16_tflops):
         """Time floor of the plan: each signal's multiply-adds at the peak of
-        the unit that runs it (FP32 FMA, or six bf16 products per output on
-        the tensor cores)."""
+        the unit that runs it (FP32 FMA, or the form's products per output on
+        the tensor cores: six for BF16X6, three for FP16X3 -- AUTO -- and
+        BF16X3)."""
         thr, _ = self.plan.tensor_cores()
         n_out = self.plan.n_out
         tc = (self.k >= thr) & (n_out >= 16384) if thr else np.zeros(len(self.k), bool)
         fl = 2.0 * n_out.astype(np.float64) * self.k
-        return 1e3 * (fl[~tc].sum() / (fp32_tflops * 1e12) + 6 * fl[tc].sum() / (bf16_tflops * 1e12))
+        prods = 6 if self.precision == self.S.Precision.BF16X6 else 3
+        return 1e3 * (fl[~tc].sum() / (fp32_tflops * 1e12) +
+                      prods * fl[tc].sum() / (bf16_tflops * 1e12))
 
     def prepare(self):
         """Records the plan's launch (work-counter reset + persistent kernel)

@@ -140,16 +140,31 @@ __device__ __forceinline__ float pow2f(int e) {  // 2^e, e in [-126, 127]
     return __int_as_float((e + 127) << 23);
 }
 
-// Max |v| over the finite values of v[0, len), ORed into *out as bits (the
-// order of non-negative floats is the order of their bit patterns).
+__device__ __forceinline__ unsigned finite_abs_max(unsigned m, float f) {
+    const unsigned b = __float_as_uint(f) & 0x7fffffffu;
+    return (b < 0x7f800000u && b > m) ? b : m;
+}
+
+// Max |v| over the finite values of v[0, len), folded into *out as bits
+// with atomicMax (the order of non-negative floats is the order of their
+// bit patterns).  16-byte loads from the first 16-byte boundary on.
 __device__ __forceinline__ void absmax_segment(const float* __restrict__ v, int64_t len,
                                                unsigned* out) {
     unsigned m = 0u;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const unsigned b = __float_as_uint(__ldg(v + i)) & 0x7fffffffu;
-        if (b < 0x7f800000u && b > m) m = b;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nt = (int64_t)gridDim.x * blockDim.x;
+    int64_t head = (int64_t)(((16u - (unsigned)(reinterpret_cast<uintptr_t>(v) & 15u)) & 15u) / 4u);
+    if (head > len) head = len;
+    if (t < head) m = finite_abs_max(m, __ldg(v + t));
+    const float4* __restrict__ v4 = reinterpret_cast<const float4*>(v + head);
+    const int64_t n4 = (len - head) / 4;
+    for (int64_t i = t; i < n4; i += nt) {
+        const float4 q = __ldg(v4 + i);
+        m = finite_abs_max(finite_abs_max(m, q.x), q.y);
+        m = finite_abs_max(finite_abs_max(m, q.z), q.w);
     }
+    const int64_t tail = head + 4 * n4 + t;
+    if (tail < len) m = finite_abs_max(m, __ldg(v + tail));
     m = __reduce_max_sync(0xffffffffu, m);
     if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
 }
@@ -211,12 +226,18 @@ __global__ void split_signal_kernel(const float* __restrict__ x, int64_t ld_x, i
     for (int64_t b = blockIdx.y; b < batch; b += gridDim.y) {
         const float* __restrict__ xr = x + b * ld_x;
         const float scale = F16 ? pow2f(f16_shift(mx[b])) : 1.0f;
+        const bool al = (reinterpret_cast<uintptr_t>(xr) & 15u) == 0;
         for (int64_t gi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gi < groups;
              gi += (int64_t)gridDim.x * blockDim.x) {
             const int64_t i0 = gi * 4;
             float e[4];
+            if (al && i0 + 4 <= n) {
+                const float4 q = __ldg(reinterpret_cast<const float4*>(xr + i0));
+                e[0] = q.x, e[1] = q.y, e[2] = q.z, e[3] = q.w;
+            } else {
 #pragma unroll
-            for (int j = 0; j < 4; ++j) e[j] = i0 + j < n ? __ldg(xr + i0 + j) : 0.0f;
+                for (int j = 0; j < 4; ++j) e[j] = i0 + j < n ? __ldg(xr + i0 + j) : 0.0f;
+            }
             uint2 t3[3];
             if (F16)
                 split4_f16(make_float4(e[0], e[1], e[2], e[3]), scale, t3);
