@@ -64,7 +64,7 @@ def test_autotuned_fir_exact_and_auto(cuda, tmp_path):
     xb = rng.uniform(-1, 1, (128, 16384)).astype(np.float32)
     tb = (ss.firwin(1025, 0.2) * 1.0).astype(np.float32)
     choice, ms = S.autotune_fir(128, 16384, 1025, S.FirMode.LFILTER, S.Precision.AUTO)
-    assert choice in ("cuda-cores-v8", "cuda-cores-v16", "tensor-cores-bf16x6")
+    assert choice in ("cuda-cores-v8", "cuda-cores-v16", "tensor-cores-fp16x3")
     y = S.fir_batched(_dev(xb, cuda), _dev(tb, cuda), S.FirMode.LFILTER, S.Precision.AUTO)
     ref = O.fir_mode_f64(xb[::31].astype(np.float64), tb.astype(np.float64), int(S.FirMode.LFILTER))
     assert normwise_err(y.cpu().numpy()[::31], ref) < 1e-5
