@@ -231,8 +231,9 @@ SCIR_API int scir_ragged_plan_stats(const scir_ragged_plan* plan,
 SCIR_API int scir_ragged_plan_tensor_cores(const scir_ragged_plan* plan, int* min_taps,
                                            int64_t* signals);
 /* One persistent launch over every CUDA-core tile of the plan, preceded by
- * the tensor-core bucket's operand split and persistent launch when the plan
- * has one (graph-capturable: no allocation, no host synchronisation). */
+ * the tensor-core bucket's max pass (FP16X3), operand split and persistent
+ * launch when the plan has one (graph-capturable: no allocation, no host
+ * synchronisation). */
 SCIR_API int scir_fir_ragged_f32(const scir_ragged_plan* plan, const float* x,
                                  const float* taps, float* y, void* stream);
 

@@ -86,17 +86,24 @@ namespace {
 constexpr int kM = 128;          // channels per tile = TMEM lanes
 constexpr int kKC = 64;          // K per stage: one 128-byte swizzle atom of bf16
 constexpr int kPh = 8;           // output phases (Hankel row shift 8 elements)
-constexpr int kU = 128;          // rows of a phase operand = largest MMA N
-constexpr int kPhT = 2;          // phases per tile (2 accumulators each: 512 columns)
-constexpr int kGroups = kPh / kPhT;  // phase groups per window
-constexpr int kNCOL = kPh * kU;  // outputs per window
-constexpr int kWB = kKC + 8 * kU;  // tap window per phase per chunk (elements)
-constexpr uint32_t kBBytesPh = kWB * 2;
+// Tile geometry for U rows per phase operand (= the MMA's largest N).  U =
+// 128 takes two output phases per tile, U = 256 one; either way the tile's
+// two FP32 accumulators are 256 columns each and fill TMEM's 512.
+template <int U>
+struct TcShape {
+    static constexpr int kU = U;
+    static constexpr int kPhT = 256 / U;        // phases per tile
+    static constexpr int kGroups = kPh / kPhT;  // phase groups (tiles) per window
+    static constexpr int kNCOL = kPh * U;       // outputs per window
+    static constexpr int kWB = kKC + 8 * U;     // tap window per phase per chunk (elements)
+    static constexpr uint32_t kBBytesPh = kWB * 2;
+};
+using RaggedShape = TcShape<128>;  // the ragged bucket's tiles
 constexpr int kEpiWarps = 16;      // four per TMEM lane quarter
 constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr int kTmemCols = 512;
 constexpr uint32_t kABytesTerm = kM * kKC * 2;  // 16 KB
-constexpr int kCrossCol = kPhT * kU;            // first column of the cross accumulators
+constexpr int kCrossCol = 256;                  // first column of the cross accumulators
 
 // One operand element in the term planes: bf16 or fp16, by form.
 using op16 = uint16_t;
@@ -259,7 +266,7 @@ __global__ void split_signal_kernel(const float* __restrict__ x, int64_t ld_x, i
 // Tap operand planes G[t][phi][i] = term t of c[i - 8*(U-1) - phi - m]
 // (zero outside [0, k)), c = taps or reversed taps (FP16X3: times
 // 2^f16_shift(*mx)).
-template <bool F16>
+template <bool F16, int U>
 __global__ void split_taps_kernel(const float* __restrict__ taps, int64_t k, int reverse, int m,
                                   int64_t LG, int terms, const unsigned* __restrict__ mx,
                                   op16* __restrict__ G) {
@@ -269,7 +276,7 @@ __global__ void split_taps_kernel(const float* __restrict__ taps, int64_t k, int
          e += (int64_t)gridDim.x * blockDim.x) {
         const int ph = (int)(e / LG);
         const int64_t i = e % LG;
-        const int64_t ci = i - 8 * (int64_t)(kU - 1) - ph - m;
+        const int64_t ci = i - 8 * (int64_t)(U - 1) - ph - m;
         const float v = (ci >= 0 && ci < k) ? __ldg(taps + (reverse ? k - 1 - ci : ci)) : 0.0f;
         op16 t[3];
         split_tap<F16>(v, terms, scale, t);
@@ -292,13 +299,14 @@ __host__ __device__ constexpr int prod_b(int p) {
 // the K step starting at J0: rows u' whose 16 taps G_phi[8u' + J0 ..] meet
 // the non-zero range [L0, L0 + k) of G_phi.  32-bit arithmetic: the launch
 // checks keep L0 + k and every J0 below 2^31.
+template <int U>
 __device__ __forceinline__ void live_rows(int J0, int L0, int k, int& lo, int& hi) {
     const int a = L0 - J0 - 15;  // 8u' >= a
     const int b = L0 + k - J0;   // 8u' < b
     const int l = a <= 0 ? 0 : (a + 7) >> 3;
-    const int h = b <= 0 ? 0 : min((b + 7) >> 3, kU);
+    const int h = b <= 0 ? 0 : min((b + 7) >> 3, U);
     lo = l & ~15;
-    hi = min((h + 15) & ~15, kU);
+    hi = min((h + 15) & ~15, U);
 }
 
 // What one role needs to know about a tile: the signal box (tensor map and
@@ -320,7 +328,7 @@ struct TileView {
     int shc;              // FP16X3: the taps' scale exponent
 };
 
-template <bool RAGGED, bool F16>
+template <bool RAGGED, bool F16, int U>
 __device__ __forceinline__ TileView tile_view(int64_t tile, const CUtensorMap* amap,
                                               const op16* G, const TcGeom& g, float* y,
                                               int64_t ld_y, const CUtensorMap* maps,
@@ -341,12 +349,12 @@ __device__ __forceinline__ TileView tile_view(int64_t tile, const CUtensorMap* a
         v.nchunks = sg.nchunks;
         v.pg = tt.pg;
         v.vec_store = sg.vec_store & g.vec_store;  // the signal's offset and the buffer
-        v.xc0 = sg.x0 + tt.blk * kNCOL;
+        v.xc0 = sg.x0 + tt.blk * TcShape<U>::kNCOL;
         v.row0 = tt.row0;
         v.rows = sg.rows - tt.row0;
         v.ld = sg.seg;
         v.y = y + sg.y_off + (int64_t)tt.row0 * sg.seg;
-        v.o0 = (int64_t)tt.blk * kNCOL + kPhT * tt.pg;
+        v.o0 = (int64_t)tt.blk * TcShape<U>::kNCOL + TcShape<U>::kPhT * tt.pg;
         v.lim0 = sg.n_out - (int64_t)tt.row0 * sg.seg;
         v.dlim = sg.seg;
         if (F16) {  // one signal: every row has its scale
@@ -354,8 +362,8 @@ __device__ __forceinline__ TileView tile_view(int64_t tile, const CUtensorMap* a
             v.shc = f16_shift(mx[2 * (int64_t)tt.sig + 1]);
         }
     } else {
-        const int pg = (int)(tile % kGroups);
-        const int64_t w = tile / kGroups;
+        const int pg = (int)(tile % TcShape<U>::kGroups);
+        const int64_t w = tile / TcShape<U>::kGroups;
         const int64_t cg = w / g.blocks_per_cg, blk = w % g.blocks_per_cg;
         v.map = amap;
         v.G = G;
@@ -365,12 +373,12 @@ __device__ __forceinline__ TileView tile_view(int64_t tile, const CUtensorMap* a
         v.nchunks = g.nchunks;
         v.pg = pg;
         v.vec_store = g.vec_store;
-        v.xc0 = (int32_t)(g.xa0 + blk * kNCOL);
+        v.xc0 = (int32_t)(g.xa0 + blk * TcShape<U>::kNCOL);
         v.row0 = (int32_t)(cg * kM);
         v.rows = g.batch - cg * kM;
         v.ld = ld_y;
         v.y = y + cg * kM * ld_y;
-        v.o0 = blk * kNCOL + kPhT * pg;
+        v.o0 = blk * TcShape<U>::kNCOL + TcShape<U>::kPhT * pg;
         v.lim0 = g.n_out;
         v.dlim = 0;
         if (F16) {
@@ -383,8 +391,9 @@ __device__ __forceinline__ TileView tile_view(int64_t tile, const CUtensorMap* a
 }
 
 // T terms per operand: 2 (BF16X3, FP16X3) or 3 (BF16X6); F16: fp16 terms
-// of scaled operands (FP16X3), else bf16.
-template <int T, bool RAGGED, bool F16>
+// of scaled operands (FP16X3), else bf16; U rows per phase operand (128 or
+// 256, the MMA's largest N).
+template <int T, bool RAGGED, bool F16, int U>
 __global__ void __launch_bounds__(kThreads, 1)
 fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const op16* __restrict__ G,
               const TcGeom g, float* __restrict__ y, int64_t ld_y, unsigned* __restrict__ err,
@@ -392,6 +401,8 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const op16* __restrict__
               const TcTile* __restrict__ tiles, const unsigned* __restrict__ mx) {
     constexpr int NPROD = T == 2 ? 3 : 6;
     constexpr uint32_t kABytes = T * kABytesTerm;
+    constexpr int kU = U, kPhT = TcShape<U>::kPhT;
+    constexpr uint32_t kBBytesPh = TcShape<U>::kBBytesPh;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
     uint64_t* full = reinterpret_cast<uint64_t*>(base + (size_t)g.nstage * g.stage_bytes);
@@ -429,7 +440,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const op16* __restrict__
             uint32_t it = 0;
             bool ok = true;
             for (int64_t tile = blockIdx.x; ok && tile < g.n_tiles; tile += gridDim.x) {
-                const TileView v = tile_view<RAGGED, F16>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles, mx);
+                const TileView v = tile_view<RAGGED, F16, U>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles, mx);
                 for (int c = 0; c < v.nchunks; ++c, ++it) {
                     const int st = (int)(it % (uint32_t)g.nstage);
                     const uint32_t ph = (it / (uint32_t)g.nstage) & 1u;
@@ -470,7 +481,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const op16* __restrict__
             uint32_t it = 0, tcount = 0;
             bool ok = true;
             for (int64_t tile = blockIdx.x; ok && tile < g.n_tiles; tile += gridDim.x, ++tcount) {
-                const TileView v = tile_view<RAGGED, F16>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles, mx);
+                const TileView v = tile_view<RAGGED, F16, U>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles, mx);
                 // the epilogue has read (and zeroed) the accumulators of the tile before
                 if (!mbar_wait(tempty, tcount & 1u)) {
                     atomicOr(err, kErrMbarTimeout);
@@ -497,8 +508,8 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const op16* __restrict__
                     // outside a step's own range meet zero taps) -- so all its
                     // MMAs share one N and constant operand offsets
                     int lo, hi, unused_lo, unused_hi;
-                    live_rows(c * kKC + kKC - 16, L0, k32, lo, unused_hi);
-                    live_rows(c * kKC, L0 + 1, k32, unused_lo, hi);
+                    live_rows<U>(c * kKC + kKC - 16, L0, k32, lo, unused_hi);
+                    live_rows<U>(c * kKC, L0 + kPhT - 1, k32, unused_lo, hi);
                     if (hi > lo) {
                         const uint32_t idesc = idesc0 | ((uint32_t)((hi - lo) >> 3) << 17);
                         const uint64_t bdl = bd0 + (uint64_t)lo;  // row lo starts 16 * lo bytes in
@@ -529,7 +540,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const op16* __restrict__
         constexpr int kCols = kU / (kEpiWarps / 4);   // columns of a phase per warp
         constexpr int kGrp = kCols / 16;
         const int q = warp & 3;                        // TMEM lane quarter
-        const int part = (warp - 2) >> 2;              // which kCols of a phase's 128 columns
+        const int part = (warp - 2) >> 2;              // which kCols of a phase's U columns
         const int c0 = part * kCols;
         const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16);
         // the accumulators start at zero (every MMA accumulates)
@@ -545,7 +556,7 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const op16* __restrict__
         mbar_arrive(tempty);
         uint32_t tcount = 0;
         for (int64_t tile = blockIdx.x; tile < g.n_tiles; tile += gridDim.x, ++tcount) {
-            const TileView v = tile_view<RAGGED, F16>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles, mx);
+            const TileView v = tile_view<RAGGED, F16, U>(tile, &amap, G, g, y, ld_y, maps, sigs, tiles, mx);
             if (!mbar_wait(tfull, tcount & 1u)) {
                 if (lane == 0) atomicOr(err, kErrMbarTimeout);
                 break;
@@ -596,11 +607,11 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const op16* __restrict__
                 for (int gi = 0; gi < kGrp; ++gi) {
                     // column u0 + i holds output ob - 8i (and the next one)
                     const int64_t ob = o0 + 8 * (kU - 1 - (c0 + 16 * gi));
-                    if (v.vec_store && ob + kPhT <= lim) {
+                    if (kPhT == 2 && v.vec_store && ob + kPhT <= lim) {
 #pragma unroll
                         for (int i = 0; i < 16; ++i)
                             *reinterpret_cast<float2*>(yr + ob - 8 * i) =
-                                make_float2(out[gi][0][i], out[gi][1][i]);
+                                make_float2(out[gi][0][i], out[gi][kPhT - 1][i]);
                     } else {
 #pragma unroll
                         for (int i = 0; i < 16; ++i)
@@ -621,8 +632,9 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const op16* __restrict__
     }
 }
 
-template <int T, bool F16>
+template <int T, bool F16, int U>
 int launch_tc(const FirArgs& a, cudaStream_t st) {
+    using Sh = TcShape<U>;
     const DeviceInfo* info = nullptr;
     int rc = current_device(&info);
     if (rc) return rc;
@@ -633,20 +645,20 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
     g.n_out = a.n_out;
     g.batch = a.batch;
     const int64_t nA = (a.n + 7) / 8 * 8;
-    const int64_t ktot = a.k + kNCOL - 1 + g.m;
+    const int64_t ktot = a.k + Sh::kNCOL - 1 + g.m;
     g.nchunks = (int)ceil_div(ktot, kKC);
-    g.LG = (int64_t)g.nchunks * kKC + 8 * kU;
-    g.blocks_per_cg = ceil_div(a.n_out, kNCOL);
-    g.n_tiles = g.blocks_per_cg * ceil_div(a.batch, kM) * kGroups;
+    g.LG = (int64_t)g.nchunks * kKC + 8 * U;
+    g.blocks_per_cg = ceil_div(a.n_out, Sh::kNCOL);
+    g.n_tiles = g.blocks_per_cg * ceil_div(a.batch, kM) * Sh::kGroups;
     g.vec_store = ((reinterpret_cast<uintptr_t>(a.y) & 7) == 0 && (a.ld_y % 2) == 0) ? 1 : 0;
     // TMA coordinates are 32-bit: the last window's K range and the channel
     // groups must stay below 2^31
-    if (nA + 2 * kNCOL + ktot >= (1LL << 31) || ceil_div(a.batch, kM) * kM >= (1LL << 31))
+    if (nA + 2 * Sh::kNCOL + ktot >= (1LL << 31) || ceil_div(a.batch, kM) * kM >= (1LL << 31))
         return set_error(SCIR_ERR_UNSUPPORTED, "tensor-core FIR coordinates exceed 32 bits");
     unsigned* err = device_error_word();
     if (!err) return set_error(SCIR_ERR_CUDA, "device error word unavailable");
 
-    const uint32_t stage = T * kABytesTerm + T * kPhT * kBBytesPh;
+    const uint32_t stage = T * kABytesTerm + T * Sh::kPhT * Sh::kBBytesPh;
     g.stage_bytes = (stage + 1023) / 1024 * 1024;
     g.tx_bytes = stage;
     const size_t extra = 1024 + 8 * (2 * 8 + 3) + 16;
@@ -685,14 +697,14 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
         split_signal_kernel<F16><<<dim3(gx, gy), 256, 0, st>>>(a.x, a.ld_x, a.batch, a.n, nA, T,
                                                                mx, xs);
         const unsigned gt = (unsigned)std::min<int64_t>(ceil_div((int64_t)kPh * g.LG, 256), 4096);
-        split_taps_kernel<F16><<<gt, 256, 0, st>>>(a.taps, a.k, a.reverse, g.m, g.LG, T,
-                                                   F16 ? mx + a.batch : nullptr, Gs);
+        split_taps_kernel<F16, U><<<gt, 256, 0, st>>>(a.taps, a.k, a.reverse, g.m, g.LG, T,
+                                                      F16 ? mx + a.batch : nullptr, Gs);
         cudaError_t le = cudaGetLastError();
         if (le != cudaSuccess)
             rc = set_error(SCIR_ERR_CUDA, "split kernels: %s", cudaGetErrorString(le));
     }
     if (rc == SCIR_OK) {
-        auto kern = fir_tc_kernel<T, false, F16>;
+        auto kern = fir_tc_kernel<T, false, F16, U>;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) {
@@ -778,7 +790,7 @@ __global__ void split_taps_ragged_kernel(const TcSplit* __restrict__ sp, const f
          e += (int64_t)gridDim.x * blockDim.x) {
         const int ph = (int)(e / d.LG);
         const int64_t i = e % d.LG;
-        const int64_t ci = i - 8 * (int64_t)(kU - 1) - ph - d.m;
+        const int64_t ci = i - 8 * (int64_t)(RaggedShape::kU - 1) - ph - d.m;
         const float v = (ci >= 0 && ci < d.k)
                             ? __ldg(taps + d.taps_off + (d.reverse ? d.k - 1 - ci : ci))
                             : 0.0f;
@@ -792,7 +804,7 @@ __global__ void split_taps_ragged_kernel(const TcSplit* __restrict__ sp, const f
 
 // Stage sizes of the tensor-core kernel for `terms` bf16 terms.
 int tc_stages(int terms, const DeviceInfo* info, TcGeom* g, size_t* smem) {
-    const uint32_t stage = terms * kABytesTerm + terms * kPhT * kBBytesPh;
+    const uint32_t stage = terms * kABytesTerm + terms * RaggedShape::kPhT * RaggedShape::kBBytesPh;
     g->stage_bytes = (stage + 1023) / 1024 * 1024;
     g->tx_bytes = stage;
     const size_t extra = 1024 + 8 * (2 * 8 + 3) + 16;
@@ -858,9 +870,10 @@ int tc_ragged_create(const TcSigIn* in, int64_t count, int form, TcRaggedPlan** 
         TcSplit& P = sp[(size_t)i];
         const int m = (int)(((d.s % 8) + 8) % 8);
         const int64_t xa0 = d.s - m;
+        constexpr int kNCOL = RaggedShape::kNCOL;
         const int64_t ktot = d.k + kNCOL - 1 + m;
         const int nchunks = (int)ceil_div(ktot, kKC);
-        const int64_t LG = (int64_t)nchunks * kKC + 8 * kU;
+        const int64_t LG = (int64_t)nchunks * kKC + 8 * RaggedShape::kU;
         // windows per segment row: enough that the signal needs <= 128 rows
         const int64_t wpr = std::max<int64_t>(1, ceil_div(d.n_out, (int64_t)kM * kNCOL));
         const int64_t seg = wpr * kNCOL;
@@ -903,7 +916,7 @@ int tc_ragged_create(const TcSigIn* in, int64_t count, int form, TcRaggedPlan** 
         p->max_region = std::max(p->max_region, region);
         p->max_g = std::max(p->max_g, (int64_t)kPh * LG);
         for (int64_t blk = 0; blk < wpr; ++blk)
-            for (int pg = 0; pg < kGroups; ++pg) {
+            for (int pg = 0; pg < RaggedShape::kGroups; ++pg) {
                 tiles.push_back(TcTile{(int32_t)i, 0, (int32_t)blk, pg});
                 cost.push_back(nchunks);
             }
@@ -938,6 +951,7 @@ int tc_ragged_create(const TcSigIn* in, int64_t count, int form, TcRaggedPlan** 
     for (int64_t i = 0; i < count; ++i) {
         const TcSig& S = sig[(size_t)i];
         const TcSplit& P = sp[(size_t)i];
+        constexpr int kNCOL = RaggedShape::kNCOL;
         const int64_t X = (int64_t)S.x0 + (S.seg / kNCOL - 1) * kNCOL + (int64_t)S.nchunks * kKC;
         const int rc = make_tmap_3d(&maps[(size_t)i],
                                     form == kTcFp16x3 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
@@ -966,7 +980,7 @@ int tc_ragged_launch(const TcRaggedPlan* p, float* y, const DeviceInfo* info, un
     if (rc) return rc;
     g.n_tiles = p->ntiles;
     g.vec_store = (reinterpret_cast<uintptr_t>(y) & 7) == 0 ? 1 : 0;
-    auto kern = fir_tc_kernel<T, true, F16>;
+    auto kern = fir_tc_kernel<T, true, F16, RaggedShape::kU>;
     SCIR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CUtensorMap unused;
     memset(&unused, 0, sizeof(unused));
@@ -1011,12 +1025,20 @@ int tc_ragged_run(const TcRaggedPlan* p, const float* x, const float* taps, floa
                          : tc_ragged_launch<3, false>(p, y, info, err, st);
 }
 
+// Filters of at least kWideTaps taps use U = 256 (one phase per tile):
+// N = 256 MMAs read fewer operand bytes per product than N = 128 ones, which
+// pays for their twice as long ramps only when the filter is long.  Measured
+// on 1,024 x 262,144 (FP16X3 step, U = 128 / 256): 4,095 taps 4.99 / 4.79 ms,
+// 2,048 taps 3.31 / 3.94 ms, 1,024 taps 2.44 / 3.66 ms.
+constexpr int64_t kWideTaps = 3584;
+
 int launch_fir_tc(const FirArgs& a, int form, cudaStream_t st) {
     if (a.batch == 0 || a.n_out == 0) return SCIR_OK;
+    const bool wide = a.k >= kWideTaps;
     switch (form) {
-    case kTcBf16x3: return launch_tc<2, false>(a, st);
-    case kTcBf16x6: return launch_tc<3, false>(a, st);
-    case kTcFp16x3: return launch_tc<2, true>(a, st);
+    case kTcBf16x3: return wide ? launch_tc<2, false, 256>(a, st) : launch_tc<2, false, 128>(a, st);
+    case kTcBf16x6: return wide ? launch_tc<3, false, 256>(a, st) : launch_tc<3, false, 128>(a, st);
+    case kTcFp16x3: return wide ? launch_tc<2, true, 256>(a, st) : launch_tc<2, true, 128>(a, st);
     default: return set_error(SCIR_ERR_INVALID_ARG, "unknown tensor-core form %d", form);
     }
 }
