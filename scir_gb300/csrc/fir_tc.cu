@@ -159,7 +159,8 @@ __device__ __forceinline__ unsigned finite_abs_max(unsigned m, float f) {
 
 // Max |v| over the finite values of v[0, len), folded into *out as bits
 // with atomicMax (the order of non-negative floats is the order of their
-// bit patterns).  16-byte loads from the first 16-byte boundary on.
+// bit patterns).  16-byte loads from the first 16-byte boundary on, four in
+// flight per thread.
 __device__ __forceinline__ void absmax_segment(const float* __restrict__ v, int64_t len,
                                                unsigned* out) {
     unsigned m = 0u;
@@ -170,10 +171,16 @@ __device__ __forceinline__ void absmax_segment(const float* __restrict__ v, int6
     if (t < head) m = finite_abs_max(m, __ldg(v + t));
     const float4* __restrict__ v4 = reinterpret_cast<const float4*>(v + head);
     const int64_t n4 = (len - head) / 4;
-    for (int64_t i = t; i < n4; i += nt) {
-        const float4 q = __ldg(v4 + i);
-        m = finite_abs_max(finite_abs_max(m, q.x), q.y);
-        m = finite_abs_max(finite_abs_max(m, q.z), q.w);
+    for (int64_t i = t; i < n4; i += 4 * nt) {
+        float4 q[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            q[u] = i + u * nt < n4 ? __ldg(v4 + i + u * nt) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            m = finite_abs_max(finite_abs_max(m, q[u].x), q[u].y);
+            m = finite_abs_max(finite_abs_max(m, q[u].z), q[u].w);
+        }
     }
     const int64_t tail = head + 4 * n4 + t;
     if (tail < len) m = finite_abs_max(m, __ldg(v + tail));
@@ -226,39 +233,47 @@ __device__ __forceinline__ void split_tap(float v, int terms, float scale, op16 
 }
 
 // x -> term planes xs[t][b][i] = term t of x[b][i] (zero for n <= i < nA);
-// FP16X3 scales row b by 2^f16_shift(mx[b]) first.  Each thread converts 4
-// consecutive elements: the loads are coalesced across the warp and each
-// plane gets one 8-byte store.
+// FP16X3 scales row b by 2^f16_shift(mx[b]) first.  Each thread converts 8
+// consecutive elements (two 16-byte loads where the row allows) and gives
+// each plane one 16-byte store; the loads and stores are coalesced across the
+// warp.
 template <bool F16>
 __global__ void split_signal_kernel(const float* __restrict__ x, int64_t ld_x, int64_t batch,
                                     int64_t n, int64_t nA, int terms,
                                     const unsigned* __restrict__ mx, op16* __restrict__ xs) {
     const int64_t plane = batch * nA;
-    const int64_t groups = nA / 4;  // nA is a multiple of 8
+    const int64_t groups = nA / 8;  // nA is a multiple of 8
     for (int64_t b = blockIdx.y; b < batch; b += gridDim.y) {
         const float* __restrict__ xr = x + b * ld_x;
         const float scale = F16 ? pow2f(f16_shift(mx[b])) : 1.0f;
         const bool al = (reinterpret_cast<uintptr_t>(xr) & 15u) == 0;
         for (int64_t gi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gi < groups;
              gi += (int64_t)gridDim.x * blockDim.x) {
-            const int64_t i0 = gi * 4;
-            float e[4];
-            if (al && i0 + 4 <= n) {
-                const float4 q = __ldg(reinterpret_cast<const float4*>(xr + i0));
-                e[0] = q.x, e[1] = q.y, e[2] = q.z, e[3] = q.w;
+            const int64_t i0 = gi * 8;
+            float e[8];
+            if (al && i0 + 8 <= n) {
+                const float4 q0 = __ldg(reinterpret_cast<const float4*>(xr + i0));
+                const float4 q1 = __ldg(reinterpret_cast<const float4*>(xr + i0 + 4));
+                e[0] = q0.x, e[1] = q0.y, e[2] = q0.z, e[3] = q0.w;
+                e[4] = q1.x, e[5] = q1.y, e[6] = q1.z, e[7] = q1.w;
             } else {
 #pragma unroll
-                for (int j = 0; j < 4; ++j) e[j] = i0 + j < n ? __ldg(xr + i0 + j) : 0.0f;
+                for (int j = 0; j < 8; ++j) e[j] = i0 + j < n ? __ldg(xr + i0 + j) : 0.0f;
             }
-            uint2 t3[3];
-            if (F16)
-                split4_f16(make_float4(e[0], e[1], e[2], e[3]), scale, t3);
-            else
-                split4_any(make_float4(e[0], e[1], e[2], e[3]), terms, t3);
+            uint2 lo[3], hi[3];
+            if (F16) {
+                split4_f16(make_float4(e[0], e[1], e[2], e[3]), scale, lo);
+                split4_f16(make_float4(e[4], e[5], e[6], e[7]), scale, hi);
+            } else {
+                split4_any(make_float4(e[0], e[1], e[2], e[3]), terms, lo);
+                split4_any(make_float4(e[4], e[5], e[6], e[7]), terms, hi);
+            }
             const int64_t o = b * nA + i0;
 #pragma unroll
             for (int t = 0; t < 3; ++t)
-                if (t < terms) *reinterpret_cast<uint2*>(xs + t * plane + o) = t3[t];
+                if (t < terms)
+                    *reinterpret_cast<uint4*>(xs + t * plane + o) =
+                        make_uint4(lo[t].x, lo[t].y, hi[t].x, hi[t].y);
         }
     }
 }
@@ -685,12 +700,12 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
                           (uint64_t)nA * 2 * (uint64_t)a.batch, kKC, kM, 1,
                           CU_TENSOR_MAP_SWIZZLE_128B);
     if (rc == SCIR_OK) {
-        const unsigned gx = (unsigned)std::min<int64_t>(ceil_div(nA / 4, 256), 4096);
+        const unsigned gx = (unsigned)std::min<int64_t>(ceil_div(nA / 8, 256 * 4), 1024);
         const unsigned gy = (unsigned)std::min<int64_t>(a.batch, 65535);
         if (F16) {
             cudaError_t me = cudaMemsetAsync(mx, 0, sizeof(unsigned) * (size_t)(a.batch + 1), st);
             if (me != cudaSuccess) rc = set_error(SCIR_ERR_CUDA, "max reset: %s", cudaGetErrorString(me));
-            const unsigned mxg = (unsigned)std::min<int64_t>(ceil_div(a.n, 1024), 64);
+            const unsigned mxg = (unsigned)std::min<int64_t>(ceil_div(a.n, 256 * 64), 64);
             absmax_rows_kernel<<<dim3(mxg, (unsigned)std::min<int64_t>(a.batch + 1, 65535)), 256, 0,
                                  st>>>(a.x, a.ld_x, a.batch, a.n, a.taps, a.k, mx);
         }
