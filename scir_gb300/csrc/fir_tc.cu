@@ -771,23 +771,29 @@ __global__ void split_planes_ragged_kernel(const TcSplit* __restrict__ sp, const
     const TcSplit d = sp[blockIdx.y];
     const float* __restrict__ xs = x + d.x_off;
     const float scale = F16 ? pow2f(f16_shift(mx[2 * (int64_t)blockIdx.y])) : 1.0f;
-    for (int64_t e0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4; e0 < d.region;
-         e0 += (int64_t)gridDim.x * blockDim.x * 4) {
-        float v[4];
+    // 8 elements per thread (regions and plane offsets are multiples of 8):
+    // one 16-byte store per plane
+    for (int64_t e0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 8; e0 < d.region;
+         e0 += (int64_t)gridDim.x * blockDim.x * 8) {
+        float v[8];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < 8; ++j) {
             const int64_t src = e0 + j - d.pad_front;
             v[j] = (src >= 0 && src < d.n) ? __ldg(xs + src) : 0.0f;
         }
-        uint2 t3[3];
-        if (F16)
-            split4_f16(make_float4(v[0], v[1], v[2], v[3]), scale, t3);
-        else
-            split4_any(make_float4(v[0], v[1], v[2], v[3]), terms, t3);
+        uint2 lo[3], hi[3];
+        if (F16) {
+            split4_f16(make_float4(v[0], v[1], v[2], v[3]), scale, lo);
+            split4_f16(make_float4(v[4], v[5], v[6], v[7]), scale, hi);
+        } else {
+            split4_any(make_float4(v[0], v[1], v[2], v[3]), terms, lo);
+            split4_any(make_float4(v[4], v[5], v[6], v[7]), terms, hi);
+        }
 #pragma unroll
         for (int t = 0; t < 3; ++t)
             if (t < terms)
-                *reinterpret_cast<uint2*>(planes + t * plane_len + d.plane_off + e0) = t3[t];
+                *reinterpret_cast<uint4*>(planes + t * plane_len + d.plane_off + e0) =
+                    make_uint4(lo[t].x, lo[t].y, hi[t].x, hi[t].y);
     }
 }
 
@@ -1018,10 +1024,10 @@ int tc_ragged_run(const TcRaggedPlan* p, const float* x, const float* taps, floa
     const bool f16 = p->form == kTcFp16x3;
     if (f16) {
         SCIR_CUDA_TRY(cudaMemsetAsync(p->mx, 0, sizeof(unsigned) * 2 * (size_t)p->nsig, st));
-        const unsigned bm = (unsigned)std::min<int64_t>(ceil_div(p->max_region, 1024), 64);
+        const unsigned bm = (unsigned)std::min<int64_t>(ceil_div(p->max_region, 256 * 64), 64);
         absmax_ragged_kernel<<<dim3(bm, (unsigned)p->nsig, 2), 256, 0, st>>>(p->split, x, taps, p->mx);
     }
-    const unsigned bx = (unsigned)std::min<int64_t>(ceil_div(p->max_region / 4, 256), 256);
+    const unsigned bx = (unsigned)std::min<int64_t>(ceil_div(p->max_region / 8, 256 * 4), 128);
     const unsigned bt = (unsigned)std::min<int64_t>(ceil_div(p->max_g, 256), 64);
     if (f16) {
         split_planes_ragged_kernel<true><<<dim3(bx, (unsigned)p->nsig), 256, 0, st>>>(

@@ -333,7 +333,7 @@ SCIR_API int scir_ragged_plan_autotune(scir_ragged_plan* plan, const float* x, c
     if (!rc) rc = build_tiles(plan, best);
     // 2. the tap count from which signals go to the tensor cores
     if (!rc && plan->tc_form) {
-        static const int kTc[] = {256, 512, 1024, 2048, 1 << 30};
+        static const int kTc[] = {64, 128, 192, 256, 384, 512, 1024, 2048, 1 << 30};
         int best_tc = plan->tc_min_taps;
         float best_tc_t = 0.0f;
         for (int c : kTc) {
