@@ -89,7 +89,11 @@ typedef enum scir_fir_mode {
  *   BF16X3's cost.  FIR entry points only (the polyphase path has no such
  *   form: SCIR_ERR_UNSUPPORTED).
  * SCIR_PREC_AUTO: the library picks (autotuned, accuracy <= 1e-5 normwise;
- *   on the tensor cores the FP16X3 form). */
+ *   on the tensor cores the FP16X3 form).
+ * On the tensor cores an Inf or NaN sample makes NaN every output whose
+ * tile reads it (its channel's outputs within about 8*256 + k samples),
+ * since the contraction multiplies it by zero taps too; the CUDA-core forms
+ * affect only the outputs whose k-tap support contains it. */
 typedef enum scir_precision {
     SCIR_PREC_AUTO = -1,
     SCIR_PREC_REF_EXACT = 0,
