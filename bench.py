@@ -341,8 +341,9 @@ class FirLong(Workload):
                 self.S.Precision.AUTO: 3}.get(p, 1)
 
     def alg_flops(self):
-        # tensor work the split scheme needs: 2*B*n*k per product
-        return 2.0 * self.B * self.N * self.K * self.products()
+        # the algorithmic work: one multiply-add per tap and output (the split
+        # forms issue products() times this on the tensor cores)
+        return 2.0 * self.B * self.N * self.K
 
     def step(self, stream, precision=None):
         self.S.fir_batched(self.x, self.taps, self.S.FirMode.LFILTER,
@@ -569,18 +570,18 @@ class Ragged(Workload):
     def alg_flops(self):
         return 2.0 * self.plan.macs
 
-    def floor_ms(self, fp32_tflops, bf16_tflops):
-        """Time floor of the plan: each signal's multiply-adds at the peak of
-        the unit that runs it (FP32 FMA, or the form's products per output on
-        the tensor cores: six for BF16X6, three for FP16X3 -- AUTO -- and
-        BF16X3)."""
+    def floor_ms(self, fp32_tflops, bf16_tflops, hbm_gbs):
+        """Time floor of the plan: per signal the larger of its bytes (input
+        and output once) at the HBM peak and its multiply-adds at the peak of
+        the unit that runs it (FP32 FMA, or the tensor cores' bf16 rate for
+        one product), summed over the signals."""
         thr, _ = self.plan.tensor_cores()
-        n_out = self.plan.n_out
+        n_out = self.plan.n_out.astype(np.float64)
         tc = (self.k >= thr) & (n_out >= 16384) if thr else np.zeros(len(self.k), bool)
-        fl = 2.0 * n_out.astype(np.float64) * self.k
-        prods = 6 if self.precision == self.S.Precision.BF16X6 else 3
-        return 1e3 * (fl[~tc].sum() / (fp32_tflops * 1e12) +
-                      prods * fl[tc].sum() / (bf16_tflops * 1e12))
+        fl = 2.0 * n_out * self.k
+        peak = np.where(tc, bf16_tflops, fp32_tflops) * 1e12
+        by = 4.0 * (self.n.astype(np.float64) + n_out)
+        return 1e3 * float(np.maximum(fl / peak, by / (hbm_gbs * 1e9)).sum())
 
     def prepare(self):
         """Records the plan's launch (work-counter reset + persistent kernel)
@@ -945,12 +946,13 @@ def roofline(W, kern_ms, peaks, fma):
     over its mean duration, against the binding peak."""
     rl = getattr(W, "roofline_launches", W.launches_per_step)
     if W.bound == "mixed":
-        floor = W.floor_ms(fma(False), peaks["bf16_tflops"])
+        floor = W.floor_ms(fma(False), peaks["bf16_tflops"], peaks["hbm_gbs"])
         return {"bound": "mixed", "achieved": floor, "peak": kern_ms, "unit": "ms (floor vs measured)",
                 "frac": floor / kern_ms, "traffic": profile_traffic(W.name), "kernel": W.kernel,
                 "kernel_ms": kern_ms,
-                "peak_source": "per-signal floor: FP32 FMA peak measured live by scir_probe_fma_peak, "
-                               "bf16 " + peaks["source"]}
+                "peak_source": "per-signal floor max(bytes / HBM, flops / unit peak) summed: FP32 "
+                               "FMA peak measured live by scir_probe_fma_peak, HBM and bf16 " +
+                               peaks["source"]}
     if W.bound == "hbm":
         achieved = W.alg_bytes() / rl / (kern_ms / 1e3) / 1e9
         peak, unit, src = peaks["hbm_gbs"], "GB/s", peaks["source"]
@@ -962,9 +964,14 @@ def roofline(W, kern_ms, peaks, fma):
         achieved = W.alg_flops() / rl / (kern_ms / 1e3) / 1e12
         peak, unit = fma(fp64), "TFLOP/s"
         src = "measured live by scir_probe_fma_peak (" + ("FP64 DFMA" if fp64 else "FP32 FFMA") + ")"
-    return {"bound": W.bound, "achieved": achieved, "peak": peak, "unit": unit,
-            "frac": achieved / peak, "traffic": profile_traffic(W.name), "kernel": W.kernel,
-            "kernel_ms": kern_ms, "peak_source": src}
+    out = {"bound": W.bound, "achieved": achieved, "peak": peak, "unit": unit,
+           "frac": achieved / peak, "traffic": profile_traffic(W.name), "kernel": W.kernel,
+           "kernel_ms": kern_ms, "peak_source": src}
+    if W.bound == "tensor" and W.products() > 1:
+        # the split form issues products() tensor products per algorithmic one
+        out["products_issued"] = W.products()
+        out["issued_frac"] = achieved * W.products() / peak
+    return out
 
 
 def resample_record(torch, S, dev, stream, steps, peaks, fma):
