@@ -1,22 +1,23 @@
 // Batched FIR on the 5th-generation tensor cores (tcgen05, kind::f16) with
 // split bf16 or fp16 operands and FP32 accumulation in TMEM, in one pass.
 //
-// Contraction.  Outputs are grouped in windows of 1,024 (o0 .. o0+1023) and
-// split by output phase phi = r mod 8 (r = o - o0 = 8u + phi, u < 128).  For
-// one phase, with u' = 127 - u and the signal window starting at the sample
-// xa = o0 + s - m (m = s mod 8, the same for every window, so xa is a
-// multiple of 8 -- 16 bytes of bf16 -- as a TMA coordinate must be):
+// Contraction.  Outputs are grouped in windows of 8U (o0 .. o0 + 8U - 1; U =
+// 128 or 256 rows per phase operand) and split by output phase phi = r mod 8
+// (r = o - o0 = 8u + phi, u < U).  For one phase, with u' = U - 1 - u and the
+// signal window starting at the sample xa = o0 + s - m (m = s mod 8, the
+// same for every window, so xa is a multiple of 8 -- 16 bytes of 16-bit
+// terms -- as a TMA coordinate must be):
 //   y[b][o0 + r] = sum_J X[b][xa + J] * c[J - m - r]
 //                = sum_J A[b][J] * B_phi[u'][J],   B_phi[u'][J] = G_phi[8u' + J],
-//   G_phi[i] = c[i - 8*127 - phi - m]  (zero outside [0, k)).
+//   G_phi[i] = c[i - 8(U-1) - phi - m]  (zero outside [0, k)).
 // A (128 channels x 64 samples per K chunk, K-major, 128-byte swizzle) is a
-// TMA box of the signal's bf16 term planes, which a split kernel writes once
-// per call (x = x1 + x2 [+ x3]).  B_phi is a Hankel
-// matrix whose rows shift by 8 bf16 = 16 bytes: exactly the no-swizzle K-major
-// core-matrix layout with a 16-byte leading (K) offset and a 128-byte stride
-// (N) offset, so B_phi is a descriptor into a contiguous tap window in shared
-// memory -- no im2col, no Toeplitz matrix.  One MMA is M=128 (channels) x
-// N<=128 (outputs of one phase) x K=16.
+// TMA box of the signal's term planes, which a split kernel writes once per
+// call (x = x1 + x2 [+ x3]).  B_phi is a Hankel matrix whose rows shift by 8
+// elements = 16 bytes: exactly the no-swizzle K-major core-matrix layout with
+// a 16-byte leading (K) offset and a 128-byte stride (N) offset, so B_phi is
+// a descriptor into a contiguous tap window in shared memory -- no im2col,
+// no Toeplitz matrix.  One MMA is M=128 (channels) x N<=U (outputs of one
+// phase) x K=16.
 //
 // Precision.  x = x1 + x2 [+ x3] and c = c1 + c2 [+ c3] in bf16 terms;
 // BF16X3 forms x1c1 + (x1c2 + x2c1), BF16X6 adds x1c3 + x2c2 + x3c1.
@@ -26,25 +27,27 @@
 // BF16X3's MMAs.  fp16's range is narrow, so every signal row is scaled by
 // 2^e before the split (max |x| 2^e < 2^15, from a max pass over the row's
 // finite samples) and the taps by their own 2^f; the epilogue multiplies by
-// 2^-(e+f), which is exact.  The
-// dominant x1c1 and the sum of the cross terms go to two separate FP32
-// accumulators (cross terms added into the large x1c1 sum would be rounded
-// against its magnitude; kept apart they are rounded against their own,
-// 2^-8 smaller, one), and the epilogue adds the two.  Both accumulators of
-// a tile's two phases fill TMEM's 512 columns.
+// 2^-(e+f), which is exact.  The dominant x1c1 and the sum of the cross terms
+// go to two separate FP32 accumulators (cross terms added into the large
+// x1c1 sum would be rounded against its magnitude; kept apart they are
+// rounded against their own, smaller, one), and the epilogue adds the two.
+// A tile's two 256-column accumulators fill TMEM's 512 columns.
 //
-// Ramps.  In the first and last ~16 K chunks of a window only some rows of
-// a phase operand meet non-zero taps; the MMAs of such a chunk cover just
-// the 16-row groups live at some K step of the chunk in either phase (N = 16
-// .. 128, B and D offset to the first live group).  The accumulators are
-// zeroed by the epilogue after it reads them, so every MMA accumulates and
-// columns a ramp MMA skips stay zero.  Measured on 1,024 x 262,144 x 4,095
-// (FP16X3 step): per-step live rows 5.50 ms, one row range per chunk 4.98 ms
-// -- the single issuing thread, not the tensor pipe, was the limit.
+// Ramps.  In the first and last 2U/16 K chunks of a window only some rows
+// of a phase operand meet non-zero taps; the MMAs of such a chunk cover just
+// the 16-row groups live at some K step of the chunk in any of the tile's
+// phases (N = 16 .. U, B and D offset to the first live group).  The
+// accumulators are zeroed by the epilogue after it reads them, so every MMA
+// accumulates and columns a ramp MMA skips stay zero.  Measured on 1,024 x
+// 262,144 x 4,095 (FP16X3 step, U = 128): live rows per K step 5.50 ms, one
+// row range per chunk 4.98 ms -- the single issuing thread, not the tensor
+// pipe, was the limit.
 //
-// Tiles.  A tile is (128 channels, one window, two phases); the four phase
-// groups of a window are consecutive tile indices, so they run on
-// neighbouring SMs at the same time and share the signal rows in L2.
+// Tiles.  A tile is (128 channels, one window, 256/U phases); the 8U/256
+// phase groups of a window are consecutive tile indices, so they run on
+// neighbouring SMs at the same time and share the signal rows in L2.  Long
+// filters take U = 256 (N = 256 MMAs read fewer operand bytes per product),
+// shorter ones U = 128 (half the ramp length); the ragged bucket uses 128.
 //
 // Why planes in memory rather than a split inside this kernel: the MMAs
 // read their A and B tiles from shared memory at about the rate shared
@@ -57,15 +60,16 @@
 //
 // Roles (576 threads, one CTA per SM, persistent over tiles):
 //   warp 0     TMA producer: per K chunk the signal box of every term and the
-//              tile's tap windows (two phases x terms) into an N-stage ring
+//              tile's tap windows (phases x terms) into an N-stage ring
 //              (full barrier with tx count);
 //   warp 1     one thread issues the MMAs (per K chunk one row range, N
 //              and operand base; every offset within the chunk a
 //              constant) and commits stages and tiles;
 //   warps 2-17 epilogue: tcgen05.ld of both accumulators (four warps per
-//              TMEM lane quarter, 32 columns each), the sum into registers,
-//              TMEM zeroed and released to the MMA thread, then one 8-byte
-//              store of the tile's two adjacent phases per column.
+//              TMEM lane quarter, U/4 columns each), the sum into registers,
+//              TMEM zeroed and released to the MMA thread, then the global
+//              stores (U = 128: one 8-byte store of the tile's two adjacent
+//              phases per column; U = 256: 4-byte stores).
 // Every wait is bounded; a timeout sets the device error word and the CTA
 // leaves its loops; the producer first waits (bounded) for its copies in
 // flight and the MMA thread for its MMAs, then TMEM is freed.
@@ -662,7 +666,7 @@ int launch_tc(const FirArgs& a, cudaStream_t st) {
     const int64_t nA = (a.n + 7) / 8 * 8;
     const int64_t ktot = a.k + Sh::kNCOL - 1 + g.m;
     g.nchunks = (int)ceil_div(ktot, kKC);
-    g.LG = (int64_t)g.nchunks * kKC + 8 * U;
+    g.LG = (int64_t)g.nchunks * kKC + 8 * Sh::kU;
     g.blocks_per_cg = ceil_div(a.n_out, Sh::kNCOL);
     g.n_tiles = g.blocks_per_cg * ceil_div(a.batch, kM) * Sh::kGroups;
     g.vec_store = ((reinterpret_cast<uintptr_t>(a.y) & 7) == 0 && (a.ld_y % 2) == 0) ? 1 : 0;
