@@ -88,25 +88,45 @@ int fill_uniform(float* p, int64_t count, uint32_t seed, cudaStream_t st) {
     return SCIR_OK;
 }
 
-// Mean time of `reps` calls of f after one warm-up call (CUDA events on st).
+// Time per call of f (CUDA events on st): one warm-up call and one timed call
+// that sizes the trials, then trials of max(min_reps, ~2 ms worth, <= 200)
+// calls -- three for calls under 5 ms, one above -- and the fastest trial's
+// mean (interference from other work on the device only adds time).
 template <typename F>
-int time_calls(F&& f, cudaStream_t st, int reps, float* ms) {
+int time_calls(F&& f, cudaStream_t st, int min_reps, float* ms) {
     int rc = f();
     if (rc) return rc;
     cudaEvent_t e0, e1;
     SCIR_CUDA_TRY(cudaEventCreate(&e0));
     SCIR_CUDA_TRY(cudaEventCreate(&e1));
-    cudaEventRecord(e0, st);
-    for (int r = 0; r < reps && rc == SCIR_OK; ++r) rc = f();
-    cudaEventRecord(e1, st);
-    cudaError_t ce = cudaEventSynchronize(e1);
-    float t = 0.0f;
-    if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, e0, e1);
+    auto timed = [&](int reps, float* t) -> int {
+        cudaEventRecord(e0, st);
+        int r2 = SCIR_OK;
+        for (int r = 0; r < reps && r2 == SCIR_OK; ++r) r2 = f();
+        cudaEventRecord(e1, st);
+        cudaError_t ce = cudaEventSynchronize(e1);
+        if (ce == cudaSuccess) ce = cudaEventElapsedTime(t, e0, e1);
+        if (r2) return r2;
+        if (ce != cudaSuccess)
+            return set_error(SCIR_ERR_CUDA, "autotune timing: %s", cudaGetErrorString(ce));
+        *t /= (float)reps;
+        return SCIR_OK;
+    };
+    float one = 0.0f;
+    rc = timed(1, &one);
+    int reps = min_reps;
+    if (!rc && one > 0.0f) reps = std::max(min_reps, std::min(200, (int)(2.0f / one) + 1));
+    const int trials = one < 5.0f ? 3 : 1;
+    float best = 0.0f;
+    for (int i = 0; i < trials && rc == SCIR_OK; ++i) {
+        float t = 0.0f;
+        rc = timed(reps, &t);
+        if (!rc && (i == 0 || t < best)) best = t;
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
-    if (ce != cudaSuccess) return set_error(SCIR_ERR_CUDA, "autotune timing: %s", cudaGetErrorString(ce));
-    *ms = t / (float)reps;
+    *ms = best;
     return SCIR_OK;
 }
 
