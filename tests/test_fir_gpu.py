@@ -213,11 +213,12 @@ def test_tensor_core_dc_lowpass(cuda, prec):
 
 
 @pytest.mark.parametrize("prec", [S.Precision.BF16X3, S.Precision.BF16X6, S.Precision.FP16X3])
-@pytest.mark.parametrize("k", [2, 3, 16, 17, 64, 1025])
+@pytest.mark.parametrize("k", [2, 3, 16, 17, 64, 1025, 4000])
 def test_tensor_core_unaligned_rows(cuda, prec, k):
     # x starting one float past a 16-byte boundary (scalar signal loads), an
     # odd output row stride (scalar stores), 260 channels (a partial third
-    # channel group) and 2,500 samples (a partial third output window)
+    # channel group) and 2,500 samples (a partial output window); 4,000 taps
+    # take the one-phase-per-tile shape (N = 256)
     import torch
     rng = np.random.default_rng(k)
     big = rng.uniform(-1, 1, (260, 2502)).astype(np.float32)
