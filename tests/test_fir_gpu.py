@@ -231,6 +231,40 @@ def test_tensor_core_unaligned_rows(cuda, prec, k):
     assert normwise_err(out.cpu().numpy(), ref) < TC_TOL[prec]
 
 
+@pytest.mark.parametrize("k", [1025, 4000])
+def test_tensor_core_five_groups_and_graph(cuda, k):
+    # 640 channels = 5 channel groups with one row at its own scale, rows of
+    # the first and last groups against FP64; then the same call recorded in
+    # a CUDA graph (the max pass, both splits and the persistent launch) and
+    # replayed bit for bit
+    import torch
+    rng = np.random.default_rng(k)
+    x = rng.uniform(-1, 1, (640, 6000)).astype(np.float32)
+    x[300] *= 1e4  # a row with its own scale in the second chunk
+    taps = (rng.standard_normal(k) / np.sqrt(k)).astype(np.float32)
+    rows = [0, 255, 256, 300, 639]
+    ref = O.fir_mode_f64(x[rows].astype(np.float64), taps.astype(np.float64), int(S.FirMode.LFILTER))
+    xd, td = _dev(x, cuda), _dev(taps, cuda)
+    for prec in (S.Precision.FP16X3, S.Precision.BF16X3):
+        y = S.fir_batched(xd, td, S.FirMode.LFILTER, prec).cpu().numpy()
+        for i, r in enumerate(rows):
+            assert normwise_err(y[r], ref[i]) < TC_TOL[prec], (prec, r)
+    S.init(0)
+    s = torch.cuda.Stream()
+    eager = torch.zeros((640, 6000), device=cuda)
+    out = torch.zeros_like(eager)
+    with torch.cuda.stream(s):
+        S.fir_batched(xd, td, S.FirMode.LFILTER, S.Precision.FP16X3, out=eager, stream=s)
+        s.synchronize()
+        with S.GraphCapture(s) as g:
+            S.fir_batched(xd, td, S.FirMode.LFILTER, S.Precision.FP16X3, out=out, stream=s)
+        out.fill_(float("nan"))
+        g.launch()
+        s.synchronize()
+    assert torch.equal(out, eager)
+    g.close()
+
+
 def test_tensor_core_strided_and_repeat(cuda):
     import torch
     rng = np.random.default_rng(21)
