@@ -7,8 +7,12 @@
 // loads.  Thread t computes outputs t*V .. t*V+V-1 of the tile from a sliding
 // register window: every block of V taps costs V shared loads of x, V/4
 // broadcast loads of taps and V*V FMAs.  The window array is padded by one
-// word per 32 so the stride-V lane pattern is bank-conflict free.  Outputs
-// are staged back through shared memory and stored coalesced.
+// word per 32 so the stride-V lane pattern is bank-conflict free.  The window
+// is staged from the 16-byte boundary at or below its start (16-byte loads
+// where the row is 16-byte aligned and the window inside it), and outputs go
+// back through shared memory and out with 16-byte stores where the tile is
+// whole and the row aligned: at short filters the staging, not the FMAs,
+// took most of the issue slots.
 //
 // EXACT = true reproduces the reference loop (crates/scir-gpu/src/lib.rs:
 // 1134-1152) bit for bit: taps are visited from the newest sample to the
@@ -24,7 +28,8 @@ constexpr int kFirMaxChunk = 4096;  // taps staged per pass (multiple of 16)
 
 inline size_t fir_tile_smem_bytes(int V, int chunk) {
     const int tile = kFirThreads * V;
-    return sizeof(float) * (size_t)(chunk + (tile + chunk) + (tile + chunk) / 32 + 4);
+    // + 8: the window starts up to 3 samples early and is staged in fours
+    return sizeof(float) * (size_t)(chunk + (tile + chunk) + (tile + chunk + 8) / 32 + 8);
 }
 
 __device__ __forceinline__ int fir_padi(int j) { return j + (j >> 5); }
@@ -80,7 +85,8 @@ __device__ __forceinline__ void fir_tile(float* smem, const float* __restrict__ 
 #pragma unroll
     for (int v = 0; v < V; ++v) acc[v] = 0.0f;
 
-    const int base = tid * V;
+    const int base0 = tid * V;
+    int r = 0;  // window misalignment of the current pass
     const int nchunks = (int)((k + chunk - 1) / chunk);
     for (int ci = 0; ci < nchunks; ++ci) {
         const int cidx = EXACT ? (nchunks - 1 - ci) : ci;
@@ -96,14 +102,31 @@ __device__ __forceinline__ void fir_tile(float* smem, const float* __restrict__ 
             }
             s_c[j] = c;
         }
+        // s_x[padi(i)] = x[w0 + i], w0 = the window start rounded down to a
+        // multiple of 4 (r = ws - w0 is added to every window position below)
         const int64_t ws = o0 + s + m0;
-        const int W = TILE + kcp;
-        for (int j = tid; j < W; j += kFirThreads) {
-            const int64_t p = ws + j;
-            s_x[fir_padi(j)] = (p >= 0 && p < n) ? __ldg(xr + p) : 0.0f;
+        const int64_t w0 = ws - (((ws % 4) + 4) % 4);
+        r = (int)(ws - w0);
+        const int W4 = (TILE + kcp + r + 3) / 4;  // float4 groups staged
+        if ((reinterpret_cast<uintptr_t>(xr) & 15) == 0 && w0 >= 0 && w0 + 4 * (int64_t)W4 <= n) {
+            const float4* __restrict__ x4 = reinterpret_cast<const float4*>(xr + w0);
+            for (int j4 = tid; j4 < W4; j4 += kFirThreads) {
+                const float4 q = __ldg(x4 + j4);
+                const int i = 4 * j4;
+                s_x[fir_padi(i)] = q.x;
+                s_x[fir_padi(i + 1)] = q.y;
+                s_x[fir_padi(i + 2)] = q.z;
+                s_x[fir_padi(i + 3)] = q.w;
+            }
+        } else {
+            for (int i = tid; i < 4 * W4; i += kFirThreads) {
+                const int64_t p = w0 + i;
+                s_x[fir_padi(i)] = (p >= 0 && p < n) ? __ldg(xr + p) : 0.0f;
+            }
         }
         __syncthreads();
 
+        const int base = base0 + r;
         float wa[V], wb[V];
         if (!EXACT) {
             // ascending blocks; block jb reads window positions base+jb .. base+jb+2V-2
@@ -138,11 +161,20 @@ __device__ __forceinline__ void fir_tile(float* smem, const float* __restrict__ 
 
     __syncthreads();
 #pragma unroll
-    for (int v = 0; v < V; ++v) s_x[fir_padi(base + v)] = acc[v];
+    for (int v = 0; v < V; ++v) s_x[fir_padi(base0 + v)] = acc[v];
     __syncthreads();
-    for (int j = tid; j < TILE; j += kFirThreads) {
-        const int64_t o = o0 + j;
-        if (o < n_out) yr[o] = s_x[fir_padi(j)];
+    if ((reinterpret_cast<uintptr_t>(yr + o0) & 15) == 0 && o0 + TILE <= n_out) {
+        float4* __restrict__ y4 = reinterpret_cast<float4*>(yr + o0);
+        for (int j4 = tid; j4 < TILE / 4; j4 += kFirThreads) {
+            const int i = 4 * j4;
+            y4[j4] = make_float4(s_x[fir_padi(i)], s_x[fir_padi(i + 1)], s_x[fir_padi(i + 2)],
+                                 s_x[fir_padi(i + 3)]);
+        }
+    } else {
+        for (int j = tid; j < TILE; j += kFirThreads) {
+            const int64_t o = o0 + j;
+            if (o < n_out) yr[o] = s_x[fir_padi(j)];
+        }
     }
 }
 
