@@ -226,7 +226,8 @@ SCIR_API int scir_ragged_plan_create(const scir_ragged_desc* desc, int64_t count
     rc = upload_sync(p->d_sigs, sigs.data(), sigs.size() * sizeof(RaggedSig));
     if (rc) return fail(rc);
     p->h_sigs = std::move(sigs);
-    p->smem = fir_tile_smem_bytes(16, kMaxSmemChunk);
+    // tiles of 8 and of 16 outputs per thread share the launch
+    p->smem = std::max(fir_tile_smem_bytes(16, kMaxSmemChunk), fir_tile_smem_bytes(8, kMaxSmemChunk));
     auto kern = precision == SCIR_PREC_REF_EXACT ? ragged_kernel<true> : ragged_kernel<false>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem);
     int per_sm = 0;
