@@ -1082,17 +1082,35 @@ def run_ours(args):
     for _ in range(max(1, args.warmup)):  # staging buffers, pinned pages, tuning: untimed
         W.host_step()
     torch.cuda.synchronize()
+    # the pinned-copy rate of this host right now (the link is shared with the
+    # other GPU of the superchip): the floor the host-buffer step can reach
+    floor = None
+    if h2d or d2h:
+        cc = copy_ceiling(torch, mib=256, chunks=(4,))
+        floor_s = max(h2d / (cc["h2d_4_streams_gbs"] * 1e9), d2h / (cc["d2h_4_streams_gbs"] * 1e9),
+                      (h2d + d2h) / (cc["both_4_streams_gbs"] * 1e9))
+        floor = {"value": W.samples_per_step() / floor_s / 1e9,
+                 "h2d_gbs": cc["h2d_4_streams_gbs"], "d2h_gbs": cc["d2h_4_streams_gbs"],
+                 "both_gbs": cc["both_4_streams_gbs"]}
     barrier()
+    step_s = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
+        t1 = time.perf_counter()
         W.host_step()
+        step_s.append(time.perf_counter() - t1)  # host_step returns after its copies
     torch.cuda.synchronize()
     e2e_s = torch.tensor([time.perf_counter() - t0], device=dev, dtype=torch.float64)
     if world > 1:
         dist.all_reduce(e2e_s, op=dist.ReduceOp.MAX)
     e2e_value = world * W.samples_per_step() * args.steps / float(e2e_s.item()) / 1e9
     e2e = {"value": e2e_value, "unit": W.unit, "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h} if (h2d or d2h) else None
+           "d2h_bytes_per_step": d2h,
+           "ms_per_step_median": 1e3 * statistics.median(step_s),
+           "ms_per_step_min": 1e3 * min(step_s),
+           "copy_floor": floor,
+           "of_copy_floor": e2e_value / (world * floor["value"]) if floor else None} \
+        if (h2d or d2h) else None
 
     kern_ms = statistics.mean(per_step) / getattr(W, "roofline_launches", W.launches_per_step)
     roof = roofline(W, kern_ms, peaks, fma)
