@@ -231,7 +231,9 @@ int stager_init(Stager* s) {
 // out_dev (row bytes out_row) comes back into `hout`.  Chunks hold ~64 MB;
 // `quantum` rounds the rows of a chunk up to a multiple that fills the
 // body's kernels (the tensor-core FIR tiles 128 channels) while a chunk
-// stays within 512 MB.
+// stays within 512 MB.  With three or more chunks the first and the last
+// hold half as many rows: the pipeline's first upload and last download run
+// alone, so shorter ones shorten the whole call.
 template <typename Body>
 int pipeline_rows(Stager* s, const void* hin, size_t in_row, void* hout, size_t out_row,
                   int64_t rows, Body body, int64_t quantum = 1) {
@@ -244,7 +246,23 @@ int pipeline_rows(Stager* s, const void* hin, size_t in_row, void* hout, size_t 
         if ((size_t)cq * row_bytes <= cap) cr = cq;
     }
     if (cr > rows) cr = rows;
-    const int64_t nchunks = ceil_div(rows, cr);
+    // chunk row counts: cr each, or (with three or more) a half chunk first
+    // and last
+    std::vector<int64_t> sizes;
+    if (rows > 2 * cr && cr >= 2) {
+        const int64_t h = cr / 2;
+        int64_t left = rows - h;
+        sizes.push_back(h);
+        while (left > cr + h) {
+            sizes.push_back(cr);
+            left -= cr;
+        }
+        if (left > h) sizes.push_back(left - h);
+        sizes.push_back(std::min(left, h));
+    } else {
+        for (int64_t r = 0; r < rows; r += cr) sizes.push_back(std::min(cr, rows - r));
+    }
+    const int64_t nchunks = (int64_t)sizes.size();
     const int used = (int)(nchunks < Stager::kBufs ? nchunks : Stager::kBufs);
     for (int i = 0; i < used; ++i) {
         int rc = ensure(&s->din[i], &s->cap_in[i], (size_t)cr * in_row);
@@ -256,12 +274,12 @@ int pipeline_rows(Stager* s, const void* hin, size_t in_row, void* hout, size_t 
     auto drain = [&]() {
         for (int j = 0; j < Stager::kStreams; ++j) cudaStreamSynchronize(s->st[j]);
     };
-    for (int64_t c = 0; c < nchunks; ++c) {
+    int64_t r0 = 0;
+    for (int64_t c = 0; c < nchunks; r0 += sizes[(size_t)c], ++c) {
         const int i = (int)(c % Stager::kBufs);
         const bool reuse = c >= Stager::kBufs;
         cudaStream_t s_k = s->st[2 + i];
-        const int64_t r0 = c * cr;
-        const int64_t nr = (r0 + cr <= rows) ? cr : rows - r0;
+        const int64_t nr = sizes[(size_t)c];
         // input buffer i: last read by the kernel of chunk c - kBufs
         if (reuse) SCIR_CUDA_TRY(cudaStreamWaitEvent(s_in, s->ev_k[i], 0));
         if (in_row)
