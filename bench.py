@@ -22,8 +22,8 @@ restatement of the reference's own algorithm on a bounded sample, on all
 host cores and on one.
 
 --impl reference times the reference's CPU implementation of the path (the
-C restatement of its loops; the Rust reference cannot be compiled here or on
-the GPU machine) on the host cores, without loading this package.
+C restatement of its loops; no Rust toolchain is installed to build the Rust
+reference) on the host cores, without loading this package.
 
 --probe-peaks prints the measured FP32 and FP64 FMA throughput of the GPU
 (the denominators of the CUDA-core-bound rooflines).
@@ -917,7 +917,7 @@ def run_reference(args):
             "scipy": scipy_rate(W),
             "e2e": {"value": value, "unit": W.unit, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "note": "the reference is Rust and no Rust toolchain exists here or on the GPU box; "
+            "note": "the reference is Rust and no Rust toolchain is installed on this host; "
                     "this arm times the C restatement of its CPU loop (oracle/scir_oracle.c) "
                     "on a bounded sample of the configuration per step, on all host threads; "
                     "single_core is the same loop on one thread (the reference is "

@@ -1,7 +1,7 @@
 /*
  * scir_oracle.c -- CPU oracle for the batched-filtering path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: the parity tests, the
  * smoke check and the CPU-baseline leg of bench.py call it to produce the
  * expected outputs.  The shipped library never links or calls it, and no
  * product code path falls back to it.

@@ -1,7 +1,7 @@
 """Channel sharding across ranks, exercised with two gloo ranks on the CPU:
 the union of the ranks' row ranges is the batch, and per-rank filtering plus
 gather_rows equals filtering the whole batch on one rank (the per-rank work
-here is the CPU oracle; on a GPU machine each rank would call the library)."""
+here is the CPU oracle; with one GPU per rank each rank calls the library)."""
 import os
 import socket
 
