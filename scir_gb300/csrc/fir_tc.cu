@@ -144,17 +144,23 @@ __device__ __forceinline__ void split4_any(const float4 v, int terms, uint2 (&ou
 
 // ---- FP16X3 scaling.  mx holds the bit pattern of max |v| over the finite
 // values of a row (0 for none); a row is scaled by 2^f16_shift(mx) so its
-// largest magnitude is below 2^15 (fp16 holds up to 65,504).  Shifts are
-// clamped to [-100, 100], so a sum of two is undone by two exact multiplies.
+// largest magnitude lies in [2^14, 2^15) (fp16 holds up to 65,504), whatever
+// the row's range: shifts lie in [-113, 140], applied as two power-of-two
+// factors (each within float's exponent range, so every product is exact)
+// and the sum of a row's and the taps' shifts is undone by three.
 __device__ __forceinline__ int f16_shift(unsigned maxbits) {
     if (maxbits == 0u || maxbits >= 0x7f800000u) return 0;
     const int E = (int)(maxbits >> 23);  // biased exponent: max |v| < 2^(E - 126)
-    const int sh = 141 - (E > 0 ? E : 1);
-    return sh < -100 ? -100 : sh > 100 ? 100 : sh;
+    return 141 - (E > 0 ? E : 1);
 }
 __device__ __forceinline__ float pow2f(int e) {  // 2^e, e in [-126, 127]
     return __int_as_float((e + 127) << 23);
 }
+// The two factors of 2^sh, sh in [-113, 140].
+struct Scale2 {
+    float a, b;
+};
+__device__ __forceinline__ Scale2 scale2(int sh) { return {pow2f(sh / 2), pow2f(sh - sh / 2)}; }
 
 __device__ __forceinline__ unsigned finite_abs_max(unsigned m, float f) {
     const unsigned b = __float_as_uint(f) & 0x7fffffffu;
@@ -201,8 +207,9 @@ __global__ void absmax_rows_kernel(const float* __restrict__ x, int64_t ld_x, in
 }
 
 // 4 floats times 2^e split into two fp16 terms, packed as 4 fp16 (8 bytes) each.
-__device__ __forceinline__ void split4_f16(const float4 v, float scale, uint2 (&out)[3]) {
-    const float s0 = v.x * scale, s1 = v.y * scale, s2 = v.z * scale, s3 = v.w * scale;
+__device__ __forceinline__ void split4_f16(const float4 v, Scale2 sc, uint2 (&out)[3]) {
+    const float s0 = v.x * sc.a * sc.b, s1 = v.y * sc.a * sc.b, s2 = v.z * sc.a * sc.b,
+                s3 = v.w * sc.a * sc.b;
     const __half2 a1 = __floats2half2_rn(s0, s1);
     const __half2 b1 = __floats2half2_rn(s2, s3);
     const float2 fa1 = __half22float2(a1), fb1 = __half22float2(b1);
@@ -218,9 +225,9 @@ __device__ __forceinline__ void split4_f16(const float4 v, float scale, uint2 (&
 // One tap value as its operand terms (bf16: 2 or 3 terms; fp16: 2 terms of
 // v 2^e).
 template <bool F16>
-__device__ __forceinline__ void split_tap(float v, int terms, float scale, op16 (&t)[3]) {
+__device__ __forceinline__ void split_tap(float v, int terms, Scale2 sc, op16 (&t)[3]) {
     if (F16) {
-        const float s = v * scale;
+        const float s = v * sc.a * sc.b;
         const __half h1 = __float2half_rn(s);
         t[0] = __half_as_ushort(h1);
         t[1] = __half_as_ushort(__float2half_rn(s - __half2float(h1)));
@@ -249,7 +256,7 @@ __global__ void split_signal_kernel(const float* __restrict__ x, int64_t ld_x, i
     const int64_t groups = nA / 8;  // nA is a multiple of 8
     for (int64_t b = blockIdx.y; b < batch; b += gridDim.y) {
         const float* __restrict__ xr = x + b * ld_x;
-        const float scale = F16 ? pow2f(f16_shift(mx[b])) : 1.0f;
+        const Scale2 scale = scale2(F16 ? f16_shift(mx[b]) : 0);
         const bool al = (reinterpret_cast<uintptr_t>(xr) & 15u) == 0;
         for (int64_t gi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gi < groups;
              gi += (int64_t)gridDim.x * blockDim.x) {
@@ -290,7 +297,7 @@ __global__ void split_taps_kernel(const float* __restrict__ taps, int64_t k, int
                                   int64_t LG, int terms, const unsigned* __restrict__ mx,
                                   op16* __restrict__ G) {
     const int64_t total = (int64_t)kPh * LG;
-    const float scale = F16 ? pow2f(f16_shift(*mx)) : 1.0f;
+    const Scale2 scale = scale2(F16 ? f16_shift(*mx) : 0);
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int ph = (int)(e / LG);
@@ -610,16 +617,18 @@ fir_tc_kernel(const __grid_constant__ CUtensorMap amap, const op16* __restrict__
             tc_fence_before();
             mbar_arrive(tempty);
             if (F16 && r < v.rows) {
-                // undo the scales 2^(e+f) of the row and the taps (two exact
-                // power-of-two multiplies)
+                // undo the scales 2^(e+f) of the row and the taps: e + f in
+                // [-226, 280], three power-of-two factors of one sign (so an
+                // intermediate over- or underflows only when the result does)
                 const int sh = f16_shift(v.mxr[r * v.mxs]) + v.shc;
-                const float f1 = pow2f(-(sh / 2)), f2 = pow2f(-(sh - sh / 2));
+                const int q = sh / 3;
+                const float f1 = pow2f(-q), f2 = pow2f(-(sh - 2 * q));
 #pragma unroll
                 for (int gi = 0; gi < kGrp; ++gi)
 #pragma unroll
                     for (int l = 0; l < kPhT; ++l)
 #pragma unroll
-                        for (int i = 0; i < 16; ++i) out[gi][l][i] = out[gi][l][i] * f1 * f2;
+                        for (int i = 0; i < 16; ++i) out[gi][l][i] = out[gi][l][i] * f1 * f1 * f2;
             }
             if (r < v.rows) {
 #pragma unroll
@@ -774,7 +783,7 @@ __global__ void split_planes_ragged_kernel(const TcSplit* __restrict__ sp, const
                                            op16* __restrict__ planes) {
     const TcSplit d = sp[blockIdx.y];
     const float* __restrict__ xs = x + d.x_off;
-    const float scale = F16 ? pow2f(f16_shift(mx[2 * (int64_t)blockIdx.y])) : 1.0f;
+    const Scale2 scale = scale2(F16 ? f16_shift(mx[2 * (int64_t)blockIdx.y]) : 0);
     // 8 elements per thread (regions and plane offsets are multiples of 8):
     // one 16-byte store per plane
     for (int64_t e0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 8; e0 < d.region;
@@ -810,7 +819,7 @@ __global__ void split_taps_ragged_kernel(const TcSplit* __restrict__ sp, const f
     const TcSplit d = sp[blockIdx.y];
     const int64_t total = (int64_t)kPh * d.LG;
     op16* Gi = G + d.g_off;
-    const float scale = F16 ? pow2f(f16_shift(mx[2 * (int64_t)blockIdx.y + 1])) : 1.0f;
+    const Scale2 scale = scale2(F16 ? f16_shift(mx[2 * (int64_t)blockIdx.y + 1]) : 0);
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int ph = (int)(e / d.LG);

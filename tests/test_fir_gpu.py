@@ -197,6 +197,33 @@ def test_fp16x3_scaling(cuda):
         assert normwise_err(y[r], ref[r]) < TOL_FP32, r
 
 
+def test_fp16x3_extreme_range(cuda):
+    # rows at the ends of float's range: 1e36 (scaled down by 2^-113 .. so its
+    # largest sample lands in [2^14, 2^15) -- a clamped shift would overflow
+    # fp16) and 1e-36 (scaled up by about 2^134); taps of unit scale keep every
+    # output a normal float
+    rng = np.random.default_rng(8)
+    x = rng.uniform(-1, 1, (6, 12000))
+    x[0] *= 1e36
+    x[1] *= 1e-36
+    x[2] *= 1e30
+    x[3] *= 1e-30
+    x[4, 100] = 3e38  # one sample near float's maximum in an otherwise small row
+    x = x.astype(np.float32)
+    taps = (rng.standard_normal(1500) / 40).astype(np.float32)
+    ref = O.fir_mode_f64(x.astype(np.float64), taps.astype(np.float64), int(S.FirMode.LFILTER))
+    y = S.fir_batched(_dev(x, cuda), _dev(taps, cuda), S.FirMode.LFILTER,
+                      S.Precision.FP16X3).cpu().numpy()
+    for r in (0, 1, 2, 3, 5):
+        assert np.all(np.isfinite(y[r])), r
+        assert normwise_err(y[r], ref[r]) < TOL_FP32, r
+    # the 3e38 row: one scale per row, set by the spike, so the unit-size
+    # samples fall below fp16's range -- the bound is normwise, relative to
+    # the row's largest output, and holds
+    assert np.all(np.isfinite(y[4]))
+    assert normwise_err(y[4], ref[4]) < TOL_FP32
+
+
 @pytest.mark.parametrize("prec", [S.Precision.FP16X3, S.Precision.BF16X6, S.Precision.FP32])
 def test_tensor_core_dc_lowpass(cuda, prec):
     # a constant input through a low-pass filter with positive taps: every
