@@ -228,7 +228,9 @@ int stager_init(Stager* s) {
 
 // Runs `body(chunk_rows, in_dev, out_dev, stream)` over row chunks with the
 // copies around it: rows [r, r+cr) of `hin` (row bytes in_row) go to in_dev,
-// out_dev (row bytes out_row) comes back into `hout`.  Chunks hold ~64 MB;
+// out_dev (row bytes out_row) comes back into `hout`.  Chunks hold a sixth
+// of the call's bytes, kept within 4 .. 64 MB (small calls still overlap
+// their uploads, kernels and downloads);
 // `quantum` rounds the rows of a chunk up to a multiple that fills the
 // body's kernels (the tensor-core FIR tiles 128 channels) while a chunk
 // stays within 512 MB.  With three or more chunks the first and the last
@@ -237,8 +239,10 @@ int stager_init(Stager* s) {
 template <typename Body>
 int pipeline_rows(Stager* s, const void* hin, size_t in_row, void* hout, size_t out_row,
                   int64_t rows, Body body, int64_t quantum = 1) {
-    const size_t target = 64ull << 20, cap = 512ull << 20;
     const size_t row_bytes = in_row + out_row + 1;
+    const size_t cap = 512ull << 20;
+    const size_t target = std::min<size_t>(64ull << 20,
+                                           std::max<size_t>(4ull << 20, (size_t)rows * row_bytes / 6));
     int64_t cr = (int64_t)(target / row_bytes);
     if (cr < 1) cr = 1;
     if (quantum > 1) {
@@ -664,7 +668,9 @@ SCIR_API int scir_fir_batched_f32_host(const float* x, int64_t batch, int64_t n,
                                                          (const float*)dt, k, mode, precision,
                                                          (float*)dout, n_out, st);
                          },
-                         128);
+                         // whole 128-channel tiles where the tensor cores may run
+                         (k >= 512 && precision != SCIR_PREC_FP32 &&
+                          precision != SCIR_PREC_REF_EXACT) ? 128 : 1);
 }
 
 SCIR_API int scir_fir1d_batched_f32_cuda(const float* x, size_t b, size_t n, const float* taps,
