@@ -1034,13 +1034,16 @@ def run_ours(args):
     tuned = None if args.no_autotune else W.autotune()
     if hasattr(W, "prepare"):
         W.prepare()
-    for _ in range(max(3, args.warmup)):
-        W.step(stream)
-    torch.cuda.synchronize()
-    barrier()
-    torch.cuda.synchronize()
     flush = torch.empty(64 << 20, dtype=torch.float32, device=dev) if W.flush_l2 else None
     with ClockSampler(smi_index(local)) as clk:
+        # the warm-up runs after the sampler's start-up wait, so the timed
+        # steps follow busy steps rather than a ~0.3 s idle gap (at short
+        # steps the first ones after an idle gap ran ~5 % slow)
+        for _ in range(max(3, args.warmup)):
+            W.step(stream)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
         per_step = time_steps(torch, W, stream, args.steps, flush=flush)
     barrier()
     total_ms = sum(per_step)

@@ -266,6 +266,15 @@ int pipeline_rows(Stager* s, const void* hin, size_t in_row, void* hout, size_t 
     } else {
         for (int64_t r = 0; r < rows; r += cr) sizes.push_back(std::min(cr, rows - r));
     }
+    // every exit, the error ones included, waits for the work in flight: the
+    // copies read and write the caller's host arrays (and the tap upload that
+    // stage_taps queued on the upload stream reads the caller's taps)
+    struct Drain {
+        Stager* s;
+        ~Drain() {
+            for (int j = 0; j < Stager::kStreams; ++j) cudaStreamSynchronize(s->st[j]);
+        }
+    } drain{s};
     const int64_t nchunks = (int64_t)sizes.size();
     const int used = (int)(nchunks < Stager::kBufs ? nchunks : Stager::kBufs);
     for (int i = 0; i < used; ++i) {
@@ -275,9 +284,6 @@ int pipeline_rows(Stager* s, const void* hin, size_t in_row, void* hout, size_t 
         if (rc) return rc;
     }
     cudaStream_t s_in = s->st[0], s_out = s->st[1];
-    auto drain = [&]() {
-        for (int j = 0; j < Stager::kStreams; ++j) cudaStreamSynchronize(s->st[j]);
-    };
     int64_t r0 = 0;
     for (int64_t c = 0; c < nchunks; r0 += sizes[(size_t)c], ++c) {
         const int i = (int)(c % Stager::kBufs);
@@ -294,10 +300,7 @@ int pipeline_rows(Stager* s, const void* hin, size_t in_row, void* hout, size_t 
         // output buffer i: last read by the download of chunk c - kBufs
         if (reuse) SCIR_CUDA_TRY(cudaStreamWaitEvent(s_k, s->ev_out[i], 0));
         int rc = body(nr, s->din[i], s->dout[i], s_k);
-        if (rc) {
-            drain();
-            return rc;
-        }
+        if (rc) return rc;
         SCIR_CUDA_TRY(cudaEventRecord(s->ev_k[i], s_k));
         SCIR_CUDA_TRY(cudaStreamWaitEvent(s_out, s->ev_k[i], 0));
         if (out_row)
@@ -310,15 +313,16 @@ int pipeline_rows(Stager* s, const void* hin, size_t in_row, void* hout, size_t 
     return SCIR_OK;
 }
 
-// Uploads `bytes` of host data into the stager's shared tap buffer; the copy
-// is complete on return, so every pipeline stream may read it.
+// Queues the upload of `bytes` of host data into the stager's shared tap
+// buffer on the upload stream, ahead of the first chunk's upload: every kernel
+// of the pipeline waits for a chunk upload recorded after it, so it reads the
+// taps whole.  pipeline_rows, which must follow, waits for the copy on every
+// exit.  (The previous call drained every stream, so the buffer is free.)
 int stage_taps(Stager* s, const void* h, size_t bytes, void** d) {
     int rc = ensure(&s->dtaps, &s->cap_taps, bytes ? bytes : 16);
     if (rc) return rc;
-    if (bytes) {
+    if (bytes)
         SCIR_CUDA_TRY(cudaMemcpyAsync(s->dtaps, h, bytes, cudaMemcpyHostToDevice, s->st[0]));
-        SCIR_CUDA_TRY(cudaStreamSynchronize(s->st[0]));
-    }
     *d = s->dtaps;
     return SCIR_OK;
 }

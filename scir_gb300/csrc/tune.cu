@@ -15,7 +15,8 @@
 // The table is keyed by the device model (name and SM count), so a saved
 // table applies to every device of that model; scir_autotune_save/load keep
 // it in a text file.  Tuning allocates its buffers from the library's scratch
-// pool, runs on a private stream and synchronises it.
+// pool, runs on a private stream and synchronises it.  Shapes whose data fits
+// in L2 are timed with L2 flushed before every call (time_calls below).
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -88,24 +89,70 @@ int fill_uniform(float* p, int64_t count, uint32_t seed, cudaStream_t st) {
     return SCIR_OK;
 }
 
+// A buffer of twice the L2 size, written before every timed call when the
+// call's data (inputs and outputs) would otherwise stay in L2 from one call
+// to the next: a call on data that was just copied in or produced by other
+// work finds little of it in L2, and the variants differ in how well they hide
+// that latency (at 64 x 65,536 samples and 63 taps the 8-output tile wins
+// cold and loses warm).  Null when the data is larger than L2.
+struct L2Flush {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+int l2_flush_for(size_t data_bytes, cudaStream_t st, L2Flush* out) {
+    *out = L2Flush{};
+    const DeviceInfo* d = nullptr;
+    int rc = current_device(&d);
+    if (rc) return rc;
+    if (d->l2_bytes <= 0 || data_bytes >= (size_t)d->l2_bytes) return SCIR_OK;
+    out->bytes = 2 * (size_t)d->l2_bytes;
+    rc = scratch_alloc(&out->p, out->bytes, st);
+    if (rc) *out = L2Flush{};
+    return rc;
+}
+
+void l2_flush_free(L2Flush* f, cudaStream_t st) {
+    if (f->p) scratch_free(f->p, st);
+    *f = L2Flush{};
+}
+
 // Time per call of f (CUDA events on st): one warm-up call and one timed call
 // that sizes the trials, then trials of max(min_reps, ~2 ms worth, <= 200)
 // calls -- three for calls under 5 ms, one above -- and the fastest trial's
-// mean (interference from other work on the device only adds time).
+// mean (interference from other work on the device only adds time).  With a
+// flush buffer every call is timed on its own, after the buffer is written
+// (<= 50 calls a trial).
 template <typename F>
-int time_calls(F&& f, cudaStream_t st, int min_reps, float* ms) {
+int time_calls(F&& f, cudaStream_t st, int min_reps, float* ms, const L2Flush& flush) {
     int rc = f();
     if (rc) return rc;
     cudaEvent_t e0, e1;
     SCIR_CUDA_TRY(cudaEventCreate(&e0));
     SCIR_CUDA_TRY(cudaEventCreate(&e1));
     auto timed = [&](int reps, float* t) -> int {
-        cudaEventRecord(e0, st);
         int r2 = SCIR_OK;
-        for (int r = 0; r < reps && r2 == SCIR_OK; ++r) r2 = f();
-        cudaEventRecord(e1, st);
-        cudaError_t ce = cudaEventSynchronize(e1);
-        if (ce == cudaSuccess) ce = cudaEventElapsedTime(t, e0, e1);
+        cudaError_t ce = cudaSuccess;
+        if (flush.p) {
+            float sum = 0.0f;
+            for (int r = 0; r < reps && r2 == SCIR_OK && ce == cudaSuccess; ++r) {
+                ce = cudaMemsetAsync(flush.p, r & 0xff, flush.bytes, st);
+                if (ce == cudaSuccess) ce = cudaEventRecord(e0, st);
+                if (ce == cudaSuccess) r2 = f();
+                if (ce == cudaSuccess) ce = cudaEventRecord(e1, st);
+                if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+                float one = 0.0f;
+                if (ce == cudaSuccess) ce = cudaEventElapsedTime(&one, e0, e1);
+                sum += one;
+            }
+            *t = sum;
+        } else {
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < reps && r2 == SCIR_OK; ++r) r2 = f();
+            cudaEventRecord(e1, st);
+            ce = cudaEventSynchronize(e1);
+            if (ce == cudaSuccess) ce = cudaEventElapsedTime(t, e0, e1);
+        }
         if (r2) return r2;
         if (ce != cudaSuccess)
             return set_error(SCIR_ERR_CUDA, "autotune timing: %s", cudaGetErrorString(ce));
@@ -115,7 +162,8 @@ int time_calls(F&& f, cudaStream_t st, int min_reps, float* ms) {
     float one = 0.0f;
     rc = timed(1, &one);
     int reps = min_reps;
-    if (!rc && one > 0.0f) reps = std::max(min_reps, std::min(200, (int)(2.0f / one) + 1));
+    if (!rc && one > 0.0f)
+        reps = std::max(min_reps, std::min(flush.p ? 50 : 200, (int)(2.0f / one) + 1));
     const int trials = one < 5.0f ? 3 : 1;
     float best = 0.0f;
     for (int i = 0; i < trials && rc == SCIR_OK; ++i) {
@@ -217,6 +265,8 @@ SCIR_API int scir_autotune_fir(int64_t batch, int64_t n, int64_t k, int mode, in
     a.k = k;
     a.y = y;
     a.ld_y = a.n_out;
+    L2Flush flush;
+    if (!rc) rc = l2_flush_for(sizeof(float) * (size_t)(batch * (n + a.n_out)), st, &flush);
     const bool exact = precision == SCIR_PREC_REF_EXACT;
     std::vector<int> cand = {1, 2};
     if (precision == SCIR_PREC_AUTO && fir_tc_supported(a)) cand.push_back(3);
@@ -229,12 +279,13 @@ SCIR_API int scir_autotune_fir(int64_t batch, int64_t n, int64_t k, int mode, in
             [&]() -> int {
                 return c == 3 ? launch_fir_tc(a, kTcFp16x3, st) : launch_fir_simt(a, exact, st, c == 1 ? 8 : 16);
             },
-            st, 3, &t);
+            st, 3, &t, flush);
         if (!rc && (best == 0 || t < best_t)) {
             best = c;
             best_t = t;
         }
     }
+    l2_flush_free(&flush, st);
     scratch_free(x, st);
     scratch_free(taps, st);
     scratch_free(y, st);
@@ -288,6 +339,8 @@ SCIR_API int scir_autotune_resample_poly(int64_t batch, int64_t n, int up, int d
     a.y = y;
     a.ld_y = n_out;
     a.n_out = n_out;
+    L2Flush flush;
+    if (!rc) rc = l2_flush_for(sizeof(float) * (size_t)(batch * (n + n_out)), st, &flush);
     const int pmin = (int)std::max<int64_t>(1, ceil_div(upr, 32));
     int best = 0;
     float best_t = 0.0f;
@@ -295,13 +348,15 @@ SCIR_API int scir_autotune_resample_poly(int64_t batch, int64_t n, int up, int d
     for (int P = pmin; P <= pmax && !rc; ++P) {
         for (int ct = 1; ct <= (batch >= 4 ? 4 : batch >= 2 ? 2 : 1) && !rc; ct *= 2) {
             float t = 0.0f;
-            rc = time_calls([&]() -> int { return launch_poly_simt(a, st, P, ct); }, st, 3, &t);
+            rc = time_calls([&]() -> int { return launch_poly_simt(a, st, P, ct); }, st, 3, &t,
+                            flush);
             if (!rc && (best == 0 || t < best_t)) {
                 best = P * 10 + ct;
                 best_t = t;
             }
         }
     }
+    l2_flush_free(&flush, st);
     scratch_free(x, st);
     scratch_free(h, st);
     scratch_free(y, st);

@@ -128,6 +128,26 @@ def test_host_pipeline_many_chunks(cuda):
     assert np.array_equal(y[::37], O.fir1d_batched_f32(x[::37], taps))
 
 
+@pytest.mark.parametrize("pinned", [False, True], ids=["pageable", "pinned"])
+def test_host_calls_back_to_back_new_taps(cuda, pinned):
+    # the tap upload is queued on the upload stream without a wait of its own:
+    # each call must still filter with its own taps, the caller may overwrite
+    # them once a call returns, and a longer tap set grows the tap buffer
+    import torch
+    rng = np.random.default_rng(13)
+    x = rng.uniform(-1, 1, (96, 30000)).astype(np.float32)
+    tap_sets = [rng.standard_normal(k).astype(np.float32) for k in (15, 15, 63, 7, 301)]
+    buf = torch.empty(301, dtype=torch.float32, pin_memory=pinned).numpy()
+    outs = []
+    for t in tap_sets:
+        buf[:t.size] = t
+        outs.append(S.fir_batched_host(x, buf[:t.size], S.FirMode.REF_CORR,
+                                       S.Precision.REF_EXACT))
+        buf[:] = np.nan  # overwritten as soon as the call returns
+    for t, y in zip(tap_sets, outs):
+        assert np.array_equal(y[::19], O.fir1d_batched_f32(x[::19], t))
+
+
 # ---------------------------------------------------------------- tensor cores
 # BF16X6 (three bf16 terms, six products) and FP16X3 (scaled fp16 hi+lo,
 # three products, 22 significant bits per operand) must meet the FP32 bound
