@@ -19,8 +19,13 @@ fir_simt_kernel(const float* __restrict__ x, int64_t ld_x, int64_t n,
                 int64_t tiles_per_row, int chunk) {
     extern __shared__ __align__(16) float smem[];
     constexpr int TILE = kFirThreads * V;
-    const int64_t row = blockIdx.x / tiles_per_row;
-    const int64_t o0 = (blockIdx.x % tiles_per_row) * (int64_t)TILE;
+    // 32-bit tile decode (the launcher keeps the grid below 2^31): a 64-bit
+    // division by a runtime value is a long instruction sequence, and at short
+    // filters every instruction of a tile's bookkeeping costs FMA issue slots
+    const uint32_t tpr = (uint32_t)tiles_per_row;
+    const uint32_t rowu = blockIdx.x / tpr;
+    const int64_t row = rowu;
+    const int64_t o0 = (int64_t)(blockIdx.x - rowu * tpr) * TILE;
     fir_tile<V, EXACT>(smem, x + row * ld_x, n, taps, k, reverse, s, y + row * ld_y, n_out, o0,
                        chunk);
 }

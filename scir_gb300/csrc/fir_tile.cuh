@@ -133,7 +133,8 @@ __device__ __forceinline__ void fir_tile(float* smem, const float* __restrict__ 
     for (int v = 0; v < V; ++v) acc[v] = 0.0f;
 
     const int base0 = tid * V;
-    const int nchunks = (int)((k + chunk - 1) / chunk);
+    // one pass for filters that fit a chunk, without a 64-bit division
+    const int nchunks = k <= 0 ? 0 : k <= chunk ? 1 : (int)((k + chunk - 1) / chunk);
     for (int ci = 0; ci < nchunks; ++ci) {
         const int cidx = EXACT ? (nchunks - 1 - ci) : ci;
         const int64_t m0 = (int64_t)cidx * chunk;
