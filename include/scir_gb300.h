@@ -318,7 +318,10 @@ SCIR_API int scir_graph_destroy(scir_graph* graph);
 /* one problem shape on synthetic data of that shape (buffers from the      */
 /* library's scratch pool, a private stream, synchronised) and records the  */
 /* fastest for the current device model; later calls with exactly that     */
-/* shape use it.  `choice` receives a short description.                    */
+/* shape use it.  A shape whose inputs and outputs fit in L2 is timed one   */
+/* call at a time after a write of twice the L2 size, as it runs on data    */
+/* that was just copied in or produced elsewhere (that write needs 2 x L2   */
+/* bytes of scratch).  `choice` receives a short description.               */
 /* ----------------------------------------------------------------------- */
 
 /* Batched FIR: CUDA-core tiles of 8 or 16 outputs per thread, and for
