@@ -52,11 +52,14 @@ namespace {
 constexpr int kCH = 2 * kTT;  // channels per CTA: lane l owns rows l and l + 32
 constexpr int kLd = kTT + 1;
 
-template <int NS>
+template <int NS, int PREC, bool FF>
 struct PipeShape {
     // warps: up to 4 sections per warp (the duplicated coefficient pairs of
-    // 4 sections take 48 registers)
-    static constexpr int G = NS < 4 ? NS : NS <= 12 ? 4 : 8;
+    // 4 sections take 48 registers).  The DF2T sosfilt of 5 - 8 sections
+    // runs on 2 warps of 4 sections, 64-thread CTAs (16,384 x 131,072 on
+    // GB300: 5.63 ms against 6.41 with 4 warps of 2); the coupled form and
+    // sosfiltfilt measured slower that way (8.99 vs 8.64, 21.0 vs 18.8 ms).
+    static constexpr int G = NS < 4 ? NS : (NS == 8 && PREC == 2 && !FF) ? 2 : NS <= 12 ? 4 : 8;
     static constexpr int SPW = NS / G;         // sections per warp
     static constexpr int kRing = G + 4;        // tile slots
     static constexpr int kAhead = kRing - G;   // tiles loaded ahead of warp 0
@@ -144,10 +147,10 @@ struct PipeArgs {
 };
 
 template <int NS, int PREC, bool FF>
-__global__ void __launch_bounds__(32 * PipeShape<NS>::G, 2)
+__global__ void __launch_bounds__(32 * PipeShape<NS, PREC, FF>::G, 2)
 sos_pipe_kernel(const __grid_constant__ SosCoef sc, const PipeArgs a) {
-    constexpr int G = PipeShape<NS>::G, SPW = PipeShape<NS>::SPW;
-    constexpr int kRing = PipeShape<NS>::kRing, kAhead = PipeShape<NS>::kAhead;
+    constexpr int G = PipeShape<NS, PREC, FF>::G, SPW = PipeShape<NS, PREC, FF>::SPW;
+    constexpr int kRing = PipeShape<NS, PREC, FF>::kRing, kAhead = PipeShape<NS, PREC, FF>::kAhead;
     extern __shared__ __align__(16) float smem_tiles[];
     float(*tiles)[kCH][kLd] = reinterpret_cast<float(*)[kCH][kLd]>(smem_tiles);  // [slot][row][time]
     __shared__ uint64_t done[G][kRing];
@@ -441,12 +444,12 @@ int run_pipe(const SosCoef& c, const PipeArgs& a, cudaStream_t st) {
     // One CTA per 64 channels, each with a (G + 4)-slot ring of 64 x 33
     // floats (68 KB for 4 warps): ask for the largest shared-memory carveout
     // so two CTAs fit an SM.
-    const size_t smem = sizeof(float) * (size_t)PipeShape<NS>::kRing * kCH * kLd;
+    const size_t smem = sizeof(float) * (size_t)PipeShape<NS, PREC, FF>::kRing * kCH * kLd;
     auto kern = sos_pipe_kernel<NS, PREC, FF>;
     SCIR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     SCIR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                        (int)cudaSharedmemCarveoutMaxShared));
-    kern<<<(unsigned)grid, 32 * PipeShape<NS>::G, smem, st>>>(c, a);
+    kern<<<(unsigned)grid, 32 * PipeShape<NS, PREC, FF>::G, smem, st>>>(c, a);
     SCIR_LAUNCH_CHECK("sos_pipe_kernel");
     return SCIR_OK;
 }
