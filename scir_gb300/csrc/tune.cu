@@ -93,8 +93,8 @@ int fill_uniform(float* p, int64_t count, uint32_t seed, cudaStream_t st) {
 // call's data (inputs and outputs) would otherwise stay in L2 from one call
 // to the next: a call on data that was just copied in or produced by other
 // work finds little of it in L2, and the variants differ in how well they hide
-// that latency (at 64 x 65,536 samples and 63 taps the 8-output tile wins
-// cold and loses warm).  Null when the data is larger than L2.
+// that latency (at 64 x 65,536 samples and 63 taps the 16-output tile is ahead
+// warm, the two tie cold).  Null when the data is larger than L2.
 struct L2Flush {
     void* p = nullptr;
     size_t bytes = 0;
