@@ -529,6 +529,17 @@ SCIR_API int scir_resample_poly_f32_host(const float* x, int64_t batch,
                                          const float* h, int64_t kh,
                                          int precision, float* y);
 
+/* How the host-buffer entry points cut a call of `rows` rows (in_row bytes
+ * per row in, out_row out) into pipelined chunks: *count receives the number
+ * of chunks and the first min(cap, *count) row counts go to sizes.  quantum
+ * is the row multiple a chunk is rounded up to (128 for host FIR calls of
+ * >= 512 taps whose precision may use the tensor cores, else 1).  Chunks
+ * hold about a sixth of the call's bytes within 4 .. 64 MB; with three or
+ * more, the first and the last hold half as many rows.  Host arithmetic
+ * only: no device is touched. */
+SCIR_API int scir_host_chunk_plan(int64_t rows, size_t in_row, size_t out_row, int64_t quantum,
+                                  int64_t* sizes, int64_t cap, int64_t* count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -115,6 +115,19 @@ def fir1d_batched_f32_auto(x, taps, device: Device) -> np.ndarray:
     raise GpuError(ERR_UNSUPPORTED, "Device.Cpu is served by scir-gpu's own CPU loop")
 
 
+def host_chunk_plan(rows: int, in_row_bytes: int, out_row_bytes: int,
+                    quantum: int = 1) -> list:
+    """Row counts of the pipelined chunks the host-buffer entry points cut a
+    call into (host arithmetic only)."""
+    count = ctypes.c_int64(0)
+    _check(load().scir_host_chunk_plan(rows, in_row_bytes, out_row_bytes, quantum, None, 0,
+                                       ctypes.byref(count)))
+    sizes = np.zeros(max(count.value, 1), np.int64)
+    _check(load().scir_host_chunk_plan(rows, in_row_bytes, out_row_bytes, quantum, _ptr(sizes),
+                                       count.value, ctypes.byref(count)))
+    return sizes[:count.value].tolist()
+
+
 def fir_batched_host(x, taps, mode: FirMode = FirMode.LFILTER,
                      precision: Precision = Precision.AUTO, out=None) -> np.ndarray:
     """Any FIR mode/precision on host rows (pipelined copies + kernel);

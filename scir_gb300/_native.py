@@ -83,6 +83,7 @@ SIGNATURES = {
     "scir_sosfiltfilt_f32_noalloc": (_int, [_vp, _i64, _i64, _i64, _vp, _int, _int, _i64, _int,
                                             _vp, _i64, _vp]),
     "scir_fir1d_batched_f32_cuda": (_int, [_vp, _sz, _sz, _vp, _sz, _vp]),
+    "scir_host_chunk_plan": (_int, [_i64, _sz, _sz, _i64, _vp, _i64, ctypes.POINTER(_i64)]),
     "scir_fir_batched_f32_host": (_int, [_vp, _i64, _i64, _vp, _i64, _int, _int, _vp]),
     "scir_sosfilt_f64_host": (_int, [_vp, _int, _vp, _sz, _sz, _vp]),
     "scir_filtfilt_f64_host": (_int, [_vp, _int, _vp, _sz, _sz, _vp]),

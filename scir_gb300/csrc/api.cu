@@ -226,19 +226,16 @@ int stager_init(Stager* s) {
     return SCIR_OK;
 }
 
-// Runs `body(chunk_rows, in_dev, out_dev, stream)` over row chunks with the
-// copies around it: rows [r, r+cr) of `hin` (row bytes in_row) go to in_dev,
-// out_dev (row bytes out_row) comes back into `hout`.  Chunks hold a sixth
-// of the call's bytes, kept within 4 .. 64 MB (small calls still overlap
-// their uploads, kernels and downloads);
-// `quantum` rounds the rows of a chunk up to a multiple that fills the
-// body's kernels (the tensor-core FIR tiles 128 channels) while a chunk
-// stays within 512 MB.  With three or more chunks the first and the last
-// hold half as many rows: the pipeline's first upload and last download run
-// alone, so shorter ones shorten the whole call.
-template <typename Body>
-int pipeline_rows(Stager* s, const void* hin, size_t in_row, void* hout, size_t out_row,
-                  int64_t rows, Body body, int64_t quantum = 1) {
+// The row counts of the chunks a call of `rows` rows (>= 1) is cut into, and
+// the largest of them (the staging buffers' row capacity).  Chunks hold a
+// sixth of the call's bytes, kept within 4 .. 64 MB (small calls still
+// overlap their uploads, kernels and downloads); `quantum` rounds the rows of
+// a chunk up to a multiple that fills the body's kernels (the tensor-core FIR
+// tiles 128 channels) while a chunk stays within 512 MB.  With three or more
+// chunks the first and the last hold half as many rows: the pipeline's first
+// upload and last download run alone, so shorter ones shorten the whole call.
+std::vector<int64_t> chunk_plan(int64_t rows, size_t in_row, size_t out_row, int64_t quantum,
+                                int64_t* max_rows) {
     const size_t row_bytes = in_row + out_row + 1;
     const size_t cap = 512ull << 20;
     const size_t target = std::min<size_t>(64ull << 20,
@@ -266,6 +263,18 @@ int pipeline_rows(Stager* s, const void* hin, size_t in_row, void* hout, size_t 
     } else {
         for (int64_t r = 0; r < rows; r += cr) sizes.push_back(std::min(cr, rows - r));
     }
+    *max_rows = cr;
+    return sizes;
+}
+
+// Runs `body(chunk_rows, in_dev, out_dev, stream)` over the chunks of
+// chunk_plan with the copies around it: a chunk's rows of `hin` (row bytes
+// in_row) go to in_dev, out_dev (row bytes out_row) comes back into `hout`.
+template <typename Body>
+int pipeline_rows(Stager* s, const void* hin, size_t in_row, void* hout, size_t out_row,
+                  int64_t rows, Body body, int64_t quantum = 1) {
+    int64_t cr = 0;
+    const std::vector<int64_t> sizes = chunk_plan(rows, in_row, out_row, quantum, &cr);
     // every exit, the error ones included, waits for the work in flight: the
     // copies read and write the caller's host arrays (and the tap upload that
     // stage_taps queued on the upload stream reads the caller's taps)
@@ -398,6 +407,19 @@ int resample_geometry(int64_t n, int* up, int* down, int64_t* n_out) {
 using namespace scir;
 
 extern "C" {
+
+SCIR_API int scir_host_chunk_plan(int64_t rows, size_t in_row, size_t out_row, int64_t quantum,
+                                  int64_t* sizes, int64_t cap, int64_t* count) {
+    clear_error();
+    SCIR_REQUIRE(rows >= 1 && quantum >= 1 && count, SCIR_ERR_INVALID_ARG,
+                 "rows and quantum must be >= 1 and count non-NULL");
+    int64_t cr = 0;
+    const std::vector<int64_t> plan = chunk_plan(rows, in_row, out_row, quantum, &cr);
+    *count = (int64_t)plan.size();
+    SCIR_REQUIRE(sizes || cap == 0, SCIR_ERR_INVALID_ARG, "sizes is NULL");
+    for (int64_t i = 0; i < cap && i < (int64_t)plan.size(); ++i) sizes[i] = plan[(size_t)i];
+    return SCIR_OK;
+}
 
 SCIR_API int64_t scir_fir_out_len(int64_t n, int64_t k, int mode) {
     if (n < 0 || k < 0) return -1;

@@ -122,6 +122,54 @@ def test_validation_before_device():
         S.RaggedPlan([10, 20], [3, 0])
 
 
+MB = 1 << 20
+
+
+@pytest.mark.parametrize("rows,in_row,out_row,quantum", [
+    (1, 4, 4, 1),
+    (64, 65536 * 4, 65536 * 4, 1),               # 64 x 65,536 short-tap FIR call
+    (1024, 262144 * 4, 262144 * 4, 128),         # 1,024 x 262,144 long-tap FIR call
+    (256, 1048576 * 4, 1141308 * 4, 1),          # resample 160/147, 256 x 1,048,576
+    (600, 40000 * 4, 40000 * 4, 1),
+    (7, 100, 100, 128),
+    (1000, 8, 8, 1),
+    (3, 100 * MB, 100 * MB, 1),                  # rows larger than a chunk's target
+    (5000, 1 * MB, 1 * MB, 128),
+])
+def test_host_chunk_plan(rows, in_row, out_row, quantum):
+    # the host-buffer layer's chunking: every row once, whole chunks of cr rows
+    # in the middle, half-size first and last chunks when there are three or
+    # more, cr from a sixth of the call's bytes within 4 .. 64 MB (at least one
+    # row), rounded up to the quantum while a chunk stays within 512 MB
+    sizes = S.host_chunk_plan(rows, in_row, out_row, quantum)
+    assert sum(sizes) == rows and min(sizes) >= 1
+    row = in_row + out_row + 1
+    target = min(64 * MB, max(4 * MB, rows * row // 6))
+    cr = max(1, target // row)
+    if quantum > 1 and -(-cr // quantum) * quantum * row <= 512 * MB:
+        cr = -(-cr // quantum) * quantum
+    cr = min(cr, rows)
+    assert max(sizes) == cr
+    if rows > 2 * cr and cr >= 2:
+        h = cr // 2
+        assert sizes[0] == h and sizes[-1] <= h
+        assert all(s == cr for s in sizes[1:-2]) and 1 <= sizes[-2] <= cr
+    else:
+        assert all(s == cr for s in sizes[:-1])
+
+
+def test_host_chunk_plan_long_tap_call():
+    # 1,024 rows of 1 MB in and 1 MB out with 128-row tensor-core tiles: a
+    # 64-row chunk, seven of 128, a 64-row chunk
+    assert S.host_chunk_plan(1024, 1 * MB, 1 * MB, 128) == [64] + [128] * 7 + [64]
+    L = S.load()
+    n = ctypes.c_int64(-1)
+    assert L.scir_host_chunk_plan(0, 4, 4, 1, None, 0, ctypes.byref(n)) == S.ERR_INVALID_ARG
+    assert L.scir_host_chunk_plan(4, 4, 4, 0, None, 0, ctypes.byref(n)) == S.ERR_INVALID_ARG
+    assert L.scir_host_chunk_plan(4, 4, 4, 1, None, 3, ctypes.byref(n)) == S.ERR_INVALID_ARG
+    assert L.scir_host_chunk_plan(4, 4, 4, 1, None, 0, ctypes.byref(n)) == S.OK and n.value == 1
+
+
 def test_no_silent_cpu_path():
     with pytest.raises(S.GpuError) as ei:
         S.fir1d_batched_f32_auto(np.zeros((1, 4), np.float32), np.ones(3, np.float32), S.Device.Cpu)
