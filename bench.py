@@ -831,8 +831,10 @@ def calibrate_cpu(W, O, threads, target_s):
     """A bounded sample of the workload that takes about target_s on
     `threads` host threads: (rows, samples per row).  Rows grow to the
     configuration's own length first, then more rows (a multiple of the
-    thread count) are taken."""
+    thread count) are taken, up to the configuration's own channel or signal
+    count: a step never holds more than the workload."""
     full = W.cpu_row_len()
+    cap = getattr(W, "B", None) or getattr(W, "COUNT", None)
     rows, per = threads, 64
     while True:
         n, dt = W.cpu_sample(O, rows, per)
@@ -846,6 +848,8 @@ def calibrate_cpu(W, O, threads, target_s):
         per = per2
     if per >= full:
         rows = max(threads, int(round(rows * scale / threads)) * threads)
+        if cap:
+            rows = min(rows, cap)
     else:
         per = max(16, int(per * scale))
     return rows, per

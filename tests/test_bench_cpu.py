@@ -82,3 +82,50 @@ def test_profile_traffic_lines_parse():
     assert bench.profile_traffic("fir_long_4095") == pytest.approx(5675235328.0)
     assert bench.profile_traffic("resample_poly_160_147") == pytest.approx(2046622720.0)
     assert bench.profile_traffic("no_such_workload") is None
+
+
+class _FakeCpuWorkload:
+    B = 64
+
+    def __init__(self, full):
+        self.full = full
+
+    def cpu_row_len(self):
+        return self.full
+
+    def cpu_sample(self, O, rows, per):
+        return rows * per, rows * per * 1e-9  # 1 ns per sample
+
+
+def test_cpu_sample_never_exceeds_the_workload():
+    # a workload whose full size takes far less than the target: one step is
+    # the whole workload (64 full-length rows), not more rows of it
+    rows, per = bench.calibrate_cpu(_FakeCpuWorkload(65536), None, 8, 10.0)
+    assert (rows, per) == (64, 65536)
+    # a long one: full-length rows, fewer than the workload holds
+    rows, per = bench.calibrate_cpu(_FakeCpuWorkload(1 << 30), None, 8, 1.0)
+    assert rows == 8 and per < (1 << 30)
+
+
+def test_reference_arm_line():
+    # the reference arm runs the restated reference loop on the host cores
+    # and prints the benchmark's JSON line with impl = reference
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference",
+                          "--workload", "fir_short", "--steps", "2", "--warmup", "3"],
+                         capture_output=True, text=True, timeout=300, cwd=root)
+    assert out.returncode == 0, out.stderr[-2000:]
+    d = json.loads(out.stdout.strip().splitlines()[-1])
+    assert d["impl"] == "reference" and d["steps"] == 2 and d["warmup"] == 3
+    assert d["metric"] == "batched FIR Gsamples/s" and d["unit"] == "Gsamples/s"
+    assert d["value"] > 0 and d["ms_per_step"] > 0 and d["higher_is_better"] is True
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert cb["sample"].startswith("64 channels x 65536 samples")
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+    assert d["config"]["channels"] == 64
