@@ -158,6 +158,28 @@ def test_host_chunk_plan(rows, in_row, out_row, quantum):
         assert all(s == cr for s in sizes[:-1])
 
 
+def test_host_chunk_plan_random_shapes():
+    # seeded sweep: rows 1 .. 100,000, row bytes 4 B .. 256 MB, quantum 1 or 128
+    rng = np.random.default_rng(21)
+    for _ in range(300):
+        rows = int(np.exp(rng.uniform(0, np.log(100000))))
+        in_row = int(np.exp(rng.uniform(np.log(4), np.log(256 * MB))))
+        out_row = int(in_row * rng.uniform(0.5, 2.0))
+        quantum = int(rng.choice([1, 128]))
+        sizes = S.host_chunk_plan(rows, in_row, out_row, quantum)
+        cr = max(sizes)
+        assert sum(sizes) == rows and min(sizes) >= 1
+        row = in_row + out_row + 1
+        # a full chunk stays within 64 MB (or is one row), or within 512 MB
+        # when rounded up to the quantum
+        assert cr == 1 or cr * row <= (512 if quantum > 1 else 64) * MB
+        if len(sizes) >= 3 and cr >= 2:  # single-row chunks have no half size
+            assert sizes[0] == cr // 2 and sizes[-1] <= cr // 2
+            assert all(s == cr for s in sizes[1:-2])
+        else:
+            assert all(s == cr for s in sizes[:-1])
+
+
 def test_host_chunk_plan_long_tap_call():
     # 1,024 rows of 1 MB in and 1 MB out with 128-row tensor-core tiles: a
     # 64-row chunk, seven of 128, a 64-row chunk
