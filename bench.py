@@ -930,6 +930,16 @@ def run_reference(args):
     return 0
 
 
+def max_over_ranks(torch, value, dev, world):
+    """The largest of the ranks' values, on every rank (the slowest rank sets
+    the job's time); `value` itself with one rank."""
+    t = torch.tensor([float(value)], device=dev, dtype=torch.float64)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def time_steps(torch, W, stream, steps, precision=None, flush=None):
     """Per-step milliseconds of `steps` steps, CUDA events on the launch stream."""
     ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
@@ -1050,11 +1060,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         per_step = time_steps(torch, W, stream, args.steps, flush=flush)
     barrier()
-    total_ms = sum(per_step)
-    t = torch.tensor([total_ms], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms = float(t.item())
+    total_ms = max_over_ranks(torch, sum(per_step), dev, world)
     ms_step = total_ms / args.steps
     value = world * W.samples_per_step() * args.steps / (total_ms / 1e3) / 1e9
 
@@ -1107,19 +1113,15 @@ def run_ours(args):
         W.host_step()
         step_s.append(time.perf_counter() - t1)  # host_step returns after its copies
     torch.cuda.synchronize()
-    e2e_s = torch.tensor([time.perf_counter() - t0], device=dev, dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(e2e_s, op=dist.ReduceOp.MAX)
+    e2e_total_s = max_over_ranks(torch, time.perf_counter() - t0, dev, world)
     # the rate at the median step (a burst of host traffic from the other GPU
     # of the superchip slows single steps: the slowest and the total-time rate
     # are reported beside it)
-    med_s = torch.tensor([statistics.median(step_s)], device=dev, dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(med_s, op=dist.ReduceOp.MAX)
-    e2e_value = world * W.samples_per_step() / float(med_s.item()) / 1e9
+    med_s = max_over_ranks(torch, statistics.median(step_s), dev, world)
+    e2e_value = world * W.samples_per_step() / med_s / 1e9
     e2e = {"value": e2e_value, "unit": W.unit, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h,
-           "value_total_time": world * W.samples_per_step() * args.steps / float(e2e_s.item()) / 1e9,
+           "value_total_time": world * W.samples_per_step() * args.steps / e2e_total_s / 1e9,
            "ms_per_step_median": 1e3 * statistics.median(step_s),
            "ms_per_step_min": 1e3 * min(step_s),
            "ms_per_step_max": 1e3 * max(step_s),

@@ -67,3 +67,37 @@ def test_two_rank_gloo_sharding():
         p.join(120)
         assert p.exitcode == 0
     assert out[0] and out[1]
+
+
+def _max_worker(rank, world, port, out):
+    import torch
+    import torch.distributed as dist
+
+    import bench
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        # each rank's own time; every rank must get the slowest one
+        out[rank] = bench.max_over_ranks(torch, 1.5 * (rank + 1), "cpu", world)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_benchmark_time_is_the_max_over_ranks():
+    import torch
+
+    import bench
+    assert bench.max_over_ranks(torch, 2.25, "cpu", 1) == 2.25
+    ctx = mp.get_context("spawn")
+    mgr = ctx.Manager()
+    out = mgr.dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_max_worker, args=(r, 2, port, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    assert out[0] == 3.0 and out[1] == 3.0
