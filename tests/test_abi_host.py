@@ -192,6 +192,28 @@ def test_host_chunk_plan_long_tap_call():
     assert L.scir_host_chunk_plan(4, 4, 4, 1, None, 0, ctypes.byref(n)) == S.OK and n.value == 1
 
 
+def test_package_never_loads_the_oracle():
+    # the oracle is test infrastructure: importing the package and loading its
+    # library pulls in neither the oracle module nor libscir_oracle.so
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import sys, scir_gb300 as S; S.load(); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('oracle' in sys.modules, 'libscir_oracle' in maps, 'libscir_gb300' in maps)")
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                         timeout=120, cwd=root)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert out.stdout.split() == ["False", "False", "True"]
+    # and no package source names it
+    pkg = os.path.join(root, "scir_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for fn in files:
+            if fn.endswith((".py", ".cu", ".cuh", ".cpp", ".h")):
+                text = open(os.path.join(dirpath, fn)).read()
+                assert "import oracle" not in text and "libscir_oracle" not in text, fn
+
+
 def test_no_silent_cpu_path():
     with pytest.raises(S.GpuError) as ei:
         S.fir1d_batched_f32_auto(np.zeros((1, 4), np.float32), np.ones(3, np.float32), S.Device.Cpu)
