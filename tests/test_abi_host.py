@@ -214,6 +214,30 @@ def test_package_never_loads_the_oracle():
                 assert "import oracle" not in text and "libscir_oracle" not in text, fn
 
 
+def test_missing_or_foreign_library_fails_loudly():
+    # no library, or a shared object without the C ABI: NativeLibraryError,
+    # never a fallback (fresh process: the loaded library is cached)
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = """
+import _ctypes
+import scir_gb300.build as B, scir_gb300._native as N
+for path, build in (("/nonexistent/libscir_gb300.so", False), (_ctypes.__file__, True)):
+    B.LIB = path
+    try:
+        N.load(build_if_missing=build)
+        print("loaded")
+    except N.NativeLibraryError as e:
+        print("missing" if "is missing" in str(e) else "no-abi" if "does not export" in str(e)
+              else "other")
+"""
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                         timeout=120, cwd=root)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert out.stdout.split() == ["missing", "no-abi"]
+
+
 def test_no_silent_cpu_path():
     with pytest.raises(S.GpuError) as ei:
         S.fir1d_batched_f32_auto(np.zeros((1, 4), np.float32), np.ones(3, np.float32), S.Device.Cpu)
